@@ -1,0 +1,267 @@
+"""Generates the golden vectors in tests/golden/*.npz by running the reference itself.
+
+Run in a container that has the reference checkout and the reference CPU build
+(``oracle/build_ref.sh``):
+
+    python tests/golden/make_golden.py [REFERENCE_ROOT]
+
+Each case builds a seeded random PEPS with the reference's own classes, runs independent sweep
+chains with ``SweepSampling`` and measures every sample with ``Observer`` (energy + gradient),
+exactly as ``gradient_descent`` does (tetragono/tetragono/sampling_lattice/gradient.py:331-358),
+one chain per simulated MPI rank (each chain re-seeds ``TAT.random``).  It records
+
+* the site tensors: raw block storage in the reference's core order plus edge metadata, and the
+  dense array the reference itself produces with ``clear_symmetry`` (names P0, U, D, L, R);
+* the Hamiltonian terms in dictionary order, with the reference's ``tensor_element`` tables;
+* the reference's sweep order;
+* per chain and per sweep: the configuration and the sampling weight ``possibility``;
+* per sample: ws = hole(()), E_loc, and the dense holes of every site;
+* the final energy per site (with its error bar) and the gradient.
+
+The generated files are committed; tests never need the reference at run time.
+"""
+import os
+import sys
+import types
+import json
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+
+
+def install_mpi_stub():
+    """A one-process stand-in for mpi4py (the reference imports it unconditionally)."""
+    mpi4py = types.ModuleType("mpi4py")
+    MPI = types.ModuleType("mpi4py.MPI")
+
+    class Comm:
+
+        def Get_rank(self):
+            return 0
+
+        def Get_size(self):
+            return 1
+
+        def Allreduce(self, *args, **kwargs):
+            pass
+
+        def Allgather(self, send, recv):
+            recv[...] = send
+
+        def Iallreduce(self, *args, **kwargs):
+            return None
+
+        def Bcast(self, *args, **kwargs):
+            pass
+
+        def Ibcast(self, *args, **kwargs):
+            return None
+
+        def bcast(self, value, root=0):
+            return value
+
+        def allreduce(self, value, op=None):
+            return value
+
+        def Barrier(self):
+            pass
+
+    class Request:
+
+        @staticmethod
+        def Waitall(requests):
+            pass
+
+    MPI.COMM_WORLD = Comm()
+    MPI.IN_PLACE = object()
+    MPI.SUM = "sum"
+    MPI.Request = Request
+    mpi4py.MPI = MPI
+    sys.modules["mpi4py"] = mpi4py
+    sys.modules["mpi4py.MPI"] = MPI
+
+
+def setup_paths():
+    sys.path.insert(0, os.path.join(REPO, "oracle", "_ref"))
+    for sub in ("tetragono", "tetraku", "lazy_graph", "PyScalapack"):
+        sys.path.insert(0, os.path.join(REF, sub))
+
+
+install_mpi_stub()
+setup_paths()
+import TAT  # noqa: E402
+import tetragono as tet  # noqa: E402
+from tetragono.tensor_element import tensor_element  # noqa: E402
+
+ORDER = ["P0", "U", "D", "L", "R"]
+
+
+def dense_site(tensor):
+    """Dense array (P0, U, D, L, R) with extent 1 for absent legs, via the reference's own
+    ``clear_symmetry`` (which concatenates segments in edge order).  The one-dimensional
+    total-symmetry leg T of site (0, 0) carries no index and is dropped."""
+    names = [str(n) for n in tensor.names]
+    t = tensor if isinstance(tensor, TAT.No.D.Tensor) else tensor.clear_symmetry()
+    present = [n for n in ORDER if n in names]
+    extra = [n for n in names if n not in ORDER]
+    for n in extra:
+        assert t.edge_by_name(n).dimension == 1, n
+    arr = np.array(t.blocks[present + extra])
+    arr = arr.reshape(arr.shape[:len(present)])
+    shape = [arr.shape[present.index(n)] if n in present else 1 for n in ORDER]
+    return arr.reshape(shape).copy()
+
+
+def edge_meta(tensor):
+    meta = []
+    for i, name in enumerate(tensor.names):
+        edge = tensor.edges[i]
+        segs = [(int(getattr(sym, "u1", 0)) if not isinstance(sym, TAT.No.Symmetry) else 0, int(dim))
+                for sym, dim in edge.segments]
+        meta.append({"name": str(name), "arrow": bool(edge.arrow), "segments": segs})
+    return meta
+
+
+def point_index(edge, point):
+    sym, idx = point
+    return int(edge.index_by_point((sym, idx)))
+
+
+def build_lattice(kind, L1, L2, D, seed):
+    """Heisenberg antiferromagnet H = S.S (J=1) in the reference's own conventions."""
+    if kind == "no":
+        from tetraku.models import heisenberg
+        state = tet.AbstractLattice(heisenberg.abstract_state(L1, L2, J=-1))
+        state.virtual_bond["R"] = D
+        state.virtual_bond["D"] = D
+    elif kind == "u1":
+        # A Bose-U(1) Heisenberg model; tetraku ships none, so it is built here: physical charge
+        # 2Sz in {+1, -1}; H = Sz Sz + (S+ S- + S- S+)/2.
+        state = tet.AbstractState(TAT.BoseU1.D.Tensor, L1, L2)
+        state.physics_edges[...] = [(1, 1), (-1, 1)]
+        phys = state.physics_edges[0, 0, 0]
+        SS = TAT.BoseU1.D.Tensor(["I0", "I1", "O0", "O1"], [phys.conjugate(), phys.conjugate(), phys, phys]).zero_()
+        charges = [1, -1]
+        for a in range(2):
+            for b in range(2):
+                sa, sb = charges[a], charges[b]
+                SS[{"I0": (-sa, 0), "I1": (-sb, 0), "O0": (sa, 0), "O1": (sb, 0)}] = 0.25 * sa * sb
+                if a != b:
+                    SS[{"I0": (-sa, 0), "I1": (-sb, 0), "O0": (sb, 0), "O1": (sa, 0)}] = 0.5
+        state.hamiltonians["vertical_bond"] = SS
+        state.hamiltonians["horizontal_bond"] = SS
+        state = tet.AbstractLattice(state)
+        segs = [(-1, D[0]), (0, D[1]), (1, D[2])]
+        state.virtual_bond["R"] = segs
+        state.virtual_bond["D"] = segs
+    else:
+        raise ValueError(kind)
+    TAT.random.seed(seed)
+    lattice = tet.SamplingLattice(state)
+    # scale by 1/sqrt(2 D^z): z = number of virtual bonds at the site
+    for l1 in range(L1):
+        for l2 in range(L2):
+            t = lattice[l1, l2]
+            z = sum(1 for n in t.names if str(n) in ("U", "D", "L", "R"))
+            dim = D if isinstance(D, int) else sum(D)
+            lattice[l1, l2] = t * (1.0 / np.sqrt(2.0 * dim**z))
+    return lattice
+
+
+def run_case(name, kind, L1, L2, D, cut, tensor_seed, chain_seeds, n_therm, n_samples):
+    lattice = build_lattice(kind, L1, L2, D, tensor_seed)
+    out = {}
+    meta = {"name": name, "kind": kind, "L1": L1, "L2": L2, "D": D, "cut": cut, "tensor_seed": tensor_seed,
+            "chain_seeds": chain_seeds, "n_therm": n_therm, "n_samples": n_samples, "sites": {}, "terms": []}
+    for l1 in range(L1):
+        for l2 in range(L2):
+            t = lattice[l1, l2]
+            out[f"site_{l1}_{l2}_dense"] = dense_site(t)
+            out[f"site_{l1}_{l2}_storage"] = np.array(t.storage).copy()
+            meta["sites"][f"{l1},{l2}"] = edge_meta(t)
+    phys = lattice.physics_edges[0, 0, 0]
+    for ti, (positions, H) in enumerate(lattice._hamiltonians.items()):
+        table = tensor_element(H)
+        rows = []
+        for s_in, outs in table.items():
+            for s_out, value in outs.items():
+                rows.append([point_index(phys, p) for p in s_in] + [point_index(phys, p) for p in s_out] +
+                            [float(value.storage[0])])
+        out[f"term_{ti}_table"] = np.array(rows)
+        out[f"term_{ti}_storage"] = np.array(H.storage).copy()
+        meta["terms"].append({"positions": [list(p) for p in positions], "edges": edge_meta(H)})
+
+    # chains
+    neel = np.zeros((L1, L2, 1), dtype=np.int64)
+    for l1 in range(L1):
+        for l2 in range(L2):
+            neel[l1, l2, 0] = (l1 + l2) % 2
+    observer = tet.Observer(lattice, enable_energy=True, enable_gradient=True)
+    confs, poss, ws_list, eloc_list, holes_list = [], [], [], [], []
+    sweep_order = None
+    with observer:
+        for seed in chain_seeds:
+            TAT.random.seed(seed)
+            sampling = tet.SweepSampling(lattice, cut, None, None)
+            if sweep_order is None:
+                sweep_order = [[list(p) for p in ps] for ps in sampling._sweep_order]
+            sampling.configuration.import_configuration(neel)
+            c_confs, c_poss, c_ws, c_eloc, c_holes = [], [], [], [], []
+            for step in range(n_therm + n_samples):
+                possibility, configuration = sampling()
+                c_confs.append(configuration.export_configuration()[:, :, 0].copy())
+                c_poss.append(possibility)
+                if step >= n_therm:
+                    before = observer._whole_result_reweight["energy"]
+                    observer(possibility, configuration)
+                    ws = float(configuration.hole(()).storage[0])
+                    reweight = ws * ws / possibility
+                    eloc = (observer._whole_result_reweight["energy"] - before) / reweight
+                    holes = configuration.holes()
+                    c_ws.append(ws)
+                    c_eloc.append(eloc)
+                    c_holes.append(np.stack([
+                        np.stack([dense_site(holes[l1][l2]) for l2 in range(L2)]) for l1 in range(L1)
+                    ]) if _same_shapes(holes, L1, L2) else _pack_holes(holes, L1, L2))
+            confs.append(c_confs)
+            poss.append(c_poss)
+            ws_list.append(c_ws)
+            eloc_list.append(c_eloc)
+            holes_list.append(c_holes)
+    out["confs"] = np.array(confs, dtype=np.int64)
+    out["possibility"] = np.array(poss)
+    out["ws"] = np.array(ws_list)
+    out["eloc"] = np.array(eloc_list)
+    for l1 in range(L1):
+        for l2 in range(L2):
+            out[f"holes_{l1}_{l2}"] = np.array([[h[l1][l2] for h in c] for c in holes_list])
+    energy, error = observer.energy
+    out["energy"] = np.array([energy, error])
+    out["total_weight"] = np.array(observer._total_weight)
+    grad = observer.gradient
+    for l1 in range(L1):
+        for l2 in range(L2):
+            out[f"grad_{l1}_{l2}"] = dense_site(grad[l1][l2])
+    meta["sweep_order"] = sweep_order
+    out["meta"] = np.array(json.dumps(meta))
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: E/site = {energy:.12f} +- {error:.3e}, saved {os.path.getsize(path)} bytes")
+
+
+def _same_shapes(holes, L1, L2):
+    return False
+
+
+def _pack_holes(holes, L1, L2):
+    return [[dense_site(holes[l1][l2]) for l2 in range(L2)] for l1 in range(L1)]
+
+
+if __name__ == "__main__":
+    run_case("heis_no_3x3_D3_dc4", "no", 3, 3, 3, 4, 1234, [11, 12], 3, 5)
+    run_case("heis_no_4x4_D4_dc16", "no", 4, 4, 4, 16, 2024, [21, 22], 4, 6)
+    run_case("heis_no_4x4_D3_dc5", "no", 4, 4, 3, 5, 77, [31], 3, 5)
+    run_case("heis_u1_4x4_D111_dc5", "u1", 4, 4, (1, 1, 1), 5, 4321, [41, 42], 3, 5)
+    run_case("heis_u1_4x4_D222_dc8", "u1", 4, 4, (2, 2, 2), 8, 8765, [51], 2, 4)
