@@ -1,0 +1,355 @@
+"""Throughput of the sampling-lattice hot path: effective samples/s of (sweep + E_loc + gradient).
+
+One step = one sweep of every chain followed by the observation of its configuration (local
+energy, gradient holes, reweighted accumulators).  B chains run at once; a step yields B samples.
+Effective samples/s = samples/s / (2 tau_int(E_loc)), tau_int estimated from the per-chain E_loc
+series (pooled autocorrelation, Sokal window c=5).
+
+Workloads (seeded synthetic PEPS, no dataset involved):
+  heis4x4  4x4 Heisenberg (J=1), no symmetry, D=4, Dcut=16, tensors N(0,1)/sqrt(2 D^z),
+           Neel start, 64 thermalisation sweeps, 1024 chains (1024 samples per step)
+  heis8x8u1  8x8 Heisenberg, U(1) bonds {-1:2, 0:2, +1:2} (D=6), Dcut=36, blocks N(0,1),
+           Neel start (total Sz = 0), 4096 chains
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--precision fp64|fp32]
+python bench.py --impl reference ...   (the oracle restatement of the reference on host cores)
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "heis4x4": dict(L1=4, L2=4, D=4, sectors=None, cut=16, scale=True, chains=1024, therm=64),
+    "heis8x8u1": dict(L1=8, L2=8, D=6, sectors=(2, 2, 2), cut=36, scale=False, chains=4096, therm=16),
+}
+DEFAULT_WORKLOAD = "heis4x4"
+FP64_NOMINAL_GFLOPS = 1250.0
+
+
+def make_lattice(w, seed=20240601):
+    from tnsp_gb300.lattice import random_heisenberg
+    return random_heisenberg(w["L1"], w["L2"], w["D"], seed=seed, scale=w["scale"], sectors=w["sectors"])
+
+
+def tau_int(series):
+    """Integrated autocorrelation time of E_loc; series shape (n_samples, n_chains)."""
+    x = np.asarray(series, dtype=np.float64)
+    n = x.shape[0]
+    if n < 3:
+        return 0.5
+    x = x - x.mean()
+    var = (x * x).mean()
+    if var <= 0:
+        return 0.5
+    tau = 0.5
+    for t in range(1, n // 2):
+        rho = (x[:-t] * x[t:]).mean() / var
+        tau += rho
+        if t >= 5 * tau:
+            break
+    return max(tau, 0.5)
+
+
+# ---------------------------------------------------------------------------------------------
+# CPU arm: the oracle (numpy restatement of the reference path), one chain per process
+# ---------------------------------------------------------------------------------------------
+def _cpu_worker(args):
+    workload, seed, seconds, max_samples = args
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    from oracle.peps_oracle import DensePEPS, ObserverAccumulator, SweepChain
+    from tnsp_gb300.lattice import neel
+    w = WORKLOADS[workload]
+    lat = make_lattice(w)
+    peps = DensePEPS([[lat[l1, l2] for l2 in range(lat.L2)] for l1 in range(lat.L1)], list(lat._hamiltonians.items()),
+                     w["cut"])
+    chain = SweepChain(peps, neel(lat.L1, lat.L2), seed)
+    acc = ObserverAccumulator(peps)
+    t0 = time.perf_counter()
+    elocs = []
+    while time.perf_counter() - t0 < seconds and len(elocs) < max_samples:
+        poss, conf = chain.sweep()
+        _, e, _ = acc.add(poss, conf)
+        elocs.append(e)
+    return len(elocs), time.perf_counter() - t0, elocs
+
+
+def cpu_baseline(workload, seconds, cores=None):
+    import multiprocessing as mp
+    cores = cores or min(os.cpu_count() or 1, 16)
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_worker, [(workload, 1000 + i, seconds, 10**9) for i in range(cores)])
+    wall = time.perf_counter() - t0
+    n = sum(r[0] for r in res)
+    busy = max(r[1] for r in res)
+    m = min(len(r[2]) for r in res)
+    series = np.array([r[2][:m] for r in res]).T if m > 0 else np.zeros((0, cores))
+    return dict(samples=n, seconds=busy, wall=wall, cores=cores, tau=tau_int(series) if m >= 3 else None)
+
+
+# ---------------------------------------------------------------------------------------------
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [l.split(",") for l in open(self.path).read().strip().splitlines() if l.strip()]
+        except Exception:
+            return None
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 5 + i and "Active" in r[5 + i]
+                          and "Not" not in r[5 + i]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup(gpus):
+    if gpus <= 1 or "RANK" not in os.environ:
+        return 0, 1, None
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ["RANK"])
+    world = int(os.environ["WORLD_SIZE"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return rank, world, dist
+
+
+def run_ours(args):
+    import torch
+    from tnsp_gb300.engine import Sampler, TNSP_FP32, TNSP_FP64
+    from tnsp_gb300.lattice import neel
+    rank, world, dist = dist_setup(args.gpus)
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    w = WORKLOADS[args.workload]
+    B = args.chains or w["chains"]
+    lat = make_lattice(w)
+    prec = TNSP_FP32 if args.precision == "fp32" else TNSP_FP64
+    s = Sampler(lat, w["cut"], device=local)
+    seeds = np.arange(B, dtype=np.uint64) + np.uint64(7919 * (rank + 1))
+    s.init_chains(neel(lat.L1, lat.L2), seeds, precision=prec)
+    t_setup = time.perf_counter()
+    s.sweep(w["therm"] if not args.quick_therm else 2)
+    therm_s = time.perf_counter() - t_setup
+    # warm-up steps (observed, untimed)
+    s.reset_observer()
+    warm_eloc = []
+    for _ in range(args.warmup):
+        s.sweep(1, observe=True)
+        warm_eloc.append(s.read_samples(1)[0][0])
+    s.counters(reset=True)
+    # timed region: K steps, inputs resident on the device
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    elocs = []
+    kernel_ms = 0.0
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(os.path.join(tempfile.gettempdir(), f"tnsp_clocks_{rank}.csv"))
+    with clocks:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            s.sweep(1, observe=True)
+            ms, _ = s.last_timing()
+            kernel_ms += ms
+            elocs.append(s.read_samples(1)[0][0])
+        torch.cuda.synchronize()
+        t_dev = time.perf_counter() - t0
+    if dist:
+        tt = torch.tensor([t_dev], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_dev = float(tt.item())
+        dist.barrier()
+    flops = s.counters(reset=True)
+    # end-to-end through the public C ABI with host buffers: upload the tensors, sweep + observe,
+    # read the accumulators (energy scalars, Delta, E*Delta) and the per-sample record
+    n_params = int(sum(lat[l1, l2].size for l1, l2 in lat.sites()))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.upload()
+        s.sweep(1, observe=True)
+        s.read_observer(with_gradient=True)
+        s.read_samples(1)
+    torch.cuda.synchronize()
+    t_e2e = time.perf_counter() - t0
+    if dist:
+        tt = torch.tensor([t_e2e], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    series = np.array(warm_eloc + elocs)
+    tau = tau_int(series)
+    samples = B * args.steps * world
+    raw = samples / t_dev
+    value = raw / (2 * tau)
+    e2e_raw = samples / t_e2e
+    h2d = n_params * 8 + n_params * 4 + lat.L1 * lat.L2 * 4 * 4 + int(sum(len(v) for v in lat.term_arrays()[1:]) * 4)
+    d2h = 8 * 8 + 2 * n_params * 8 + 3 * B * 8 + 4
+    avg_launch_ms = kernel_ms / args.steps
+    achieved = float(flops.sum()) / args.steps / (avg_launch_ms * 1e-3) / 1e9
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu and world == 1:
+        c = cpu_baseline(args.workload, args.cpu_seconds)
+        cpu_raw = c["samples"] / c["seconds"]
+        cpu = {"value": cpu_raw / (2 * tau), "unit": "effective samples/s", "cores": c["cores"], "kind": "port",
+               "sample": (f"{c['samples']} samples: {c['cores']} single-threaded processes, one chain each from the "
+                          f"Neel state, {args.cpu_seconds:.0f} s each; raw {cpu_raw:.3f} samples/s divided by "
+                          f"2*tau_int of the GPU chains (identical chain dynamics)")}
+    scal, _, _ = s.read_observer(with_gradient=False)
+    from tnsp_gb300.engine import estimators
+    e_site = estimators(scal, lat.site_number)
+    out = {
+        "metric": "effective samples/s (E_loc + gradient) at fixed error vs FP64 oracle, 1 GB300",
+        "value": value,
+        "unit": "effective samples/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": t_dev / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64" if prec == TNSP_FP64 else "f32",
+        "data": "synthetic (seeded random PEPS, Neel start)",
+        "config": {"workload": args.workload, "lattice": f"{w['L1']}x{w['L2']}", "D": w["D"],
+                   "sectors": w["sectors"], "Dcut": w["cut"], "chains_per_gpu": B,
+                   "thermalisation_sweeps": w["therm"], "parallelism": f"replicas{world}",
+                   "l2": "working set larger than L2 (per-chain scratch slots)"},
+        "raw_samples_per_s": raw,
+        "tau_int": tau,
+        "energy_per_site": e_site[0],
+        "energy_error": e_site[1],
+        "acceptance": float(scal[7]) / max(1.0, float(scal[0])),
+        "thermalisation_s": therm_s,
+        "e2e": {"value": e2e_raw / (2 * tau), "unit": "effective samples/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "fp64", "kernel": "sweep_kernel<double>" if prec == TNSP_FP64 else "sweep_kernel<float>",
+                     "achieved": achieved, "peak": FP64_NOMINAL_GFLOPS if prec == TNSP_FP64 else None,
+                     "unit": "GFLOP/s", "frac": achieved / FP64_NOMINAL_GFLOPS if prec == TNSP_FP64 else None,
+                     "peak_source": "nominal GB300 FP64 1.25 TFLOP/s (no FP64 figure in MEASURED_PEAKS.json)",
+                     "flops_per_launch": float(flops.sum()) / args.steps,
+                     "flops_split": {"contract": flops[0] / args.steps, "qr": flops[1] / args.steps,
+                                     "svd": flops[2] / args.steps, "strip": flops[3] / args.steps},
+                     "traffic": None},
+        "cpu_baseline": cpu,
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(out))
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    w = WORKLOADS[args.workload]
+    total = 0
+    secs = 0.0
+    taus = []
+    per_step = max(5.0, args.cpu_seconds / max(1, args.steps))
+    for _ in range(args.warmup):
+        cpu_baseline(args.workload, 2.0)
+    vals = []
+    for _ in range(args.steps):
+        c = cpu_baseline(args.workload, per_step)
+        total += c["samples"]
+        secs += c["seconds"]
+        vals.append(c["samples"] / c["seconds"])
+        if c["tau"]:
+            taus.append(c["tau"])
+    tau = float(np.mean(taus)) if taus else 0.5
+    raw = total / secs
+    value = raw / (2 * tau)
+    cores = min(os.cpu_count() or 1, 16)
+    out = {
+        "metric": "effective samples/s (E_loc + gradient) at fixed error vs FP64 oracle, 1 GB300",
+        "impl": "reference",
+        "value": value,
+        "unit": "effective samples/s",
+        "n_gpus": 0,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": secs / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded random PEPS, Neel start)",
+        "config": {"workload": args.workload, "lattice": f"{w['L1']}x{w['L2']}", "D": w["D"], "sectors": w["sectors"],
+                   "Dcut": w["cut"], "parallelism": f"{cores} processes"},
+        "raw_samples_per_s": raw,
+        "tau_int": tau,
+        "cpu_baseline": {"value": value, "unit": "effective samples/s", "cores": cores, "kind": "port",
+                         "sample": f"{total} samples over {args.steps} steps of {per_step:.0f} s, one chain per "
+                                   "single-threaded process (the reference itself is not installable on the GPU box)"},
+        "e2e": {"value": value, "unit": "effective samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--chains", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--quick-therm", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

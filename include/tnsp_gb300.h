@@ -1,0 +1,138 @@
+/*
+ * tnsp_gb300: GB300-native sampling-lattice Monte Carlo over a PEPS (sweep sampling, local
+ * energy and energy gradient with boundary-MPS contraction truncated to Dcut).
+ *
+ * C ABI.  Every function returns 0 on success or a negative TNSP_E_* code; the message of the
+ * last failure of a context is returned by tnsp_last_error.  No C++ exception crosses this
+ * boundary.  One host thread per context; all device work is enqueued on the context stream.
+ *
+ * Each entry point names the reference interface it replaces (path:line in USTC-TNS/TNSP).
+ */
+#ifndef TNSP_GB300_H
+#define TNSP_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TNSP_OK 0
+#define TNSP_E_ARG (-1)        /* invalid argument or unsupported model shape */
+#define TNSP_E_CUDA (-2)       /* a CUDA runtime call failed */
+#define TNSP_E_STATE (-3)      /* call out of order (no lattice, no chains, ...) */
+#define TNSP_E_DEVICE (-4)     /* a kernel reported a failure (see the status word) */
+#define TNSP_E_NOMEM (-5)      /* device allocation failed */
+
+/* device status word bits (tnsp_device_status) */
+#define TNSP_ST_SVD_NOCONV 1   /* one-sided Jacobi hit its sweep limit */
+#define TNSP_ST_NONFINITE 2    /* a NaN/Inf amplitude or ratio appeared */
+#define TNSP_ST_UNSUPPORTED 4  /* a Hamiltonian element changes one site only */
+#define TNSP_ST_ZERO_WS 8      /* a chain's amplitude is exactly zero */
+
+typedef struct tnsp_ctx tnsp_ctx;
+
+/* precision of the tensor arithmetic inside the sampler */
+#define TNSP_FP64 0
+#define TNSP_FP32 1
+
+/*
+ * Creates a context on CUDA device `device` using stream `stream` (a cudaStream_t, or NULL for
+ * the legacy default stream).
+ * Replaces: the per-process state of TAT/PyTAT (PyTAT/PyTAT.hpp:87, the global mt19937_64) and
+ * the Configuration object graph (tetragono/tetragono/sampling_lattice/lattice.py:58-79).
+ */
+int tnsp_ctx_create(tnsp_ctx** out, int device, void* stream);
+int tnsp_ctx_destroy(tnsp_ctx* ctx);
+const char* tnsp_last_error(tnsp_ctx* ctx);
+
+/*
+ * Uploads the lattice: L1 x L2 sites, physical dimension P, the four virtual bond extents of
+ * every site (dims[(l1*L2+l2)*4 + {0:U,1:D,2:L,3:R}], 1 where the bond is absent) and the dense
+ * site tensors A[p][u][d][l][r] (float64, concatenated in row-major site order).  A block-sparse
+ * (Bose U(1)/Z2) tensor is passed densely with zeros outside its blocks; the host package
+ * converts the reference's block storage (TAT/include/TAT/structure/core.hpp:152-191).
+ * Replaces: SamplingLattice.__init__/__setitem__ (tetragono/tetragono/sampling_lattice/lattice.py:746-796)
+ * and the shrinker projection set-up (lattice.py:291-339).
+ */
+int tnsp_lattice_upload(tnsp_ctx* ctx, int L1, int L2, int P, const int* dims, const double* tensors, int cut);
+
+/*
+ * Uploads the Hamiltonian: n_terms two-site terms in the reference's dictionary order.
+ * sites[t*4 + {0,1,2,3}] = (l1, l2) of positions[0] then positions[1] of term t (nearest
+ * neighbours).  For term t and input pair index i = s0*P + s1 (s0 at positions[0]) the outputs
+ * are entries [offsets[t*P*P + i], offsets[t*P*P + i] + counts[t*P*P + i]) of out_index (o0*P + o1)
+ * and value, in the order tensor_element lists them (counts = -1: input not in the table).
+ * Replaces: tensor_element/calculate_element (tetragono/tetragono/tensor_element.py:20-108) and
+ * SweepSampling._get_proper_position_order (tetragono/tetragono/sampling_lattice/sampling.py:156-190).
+ */
+int tnsp_model_upload(tnsp_ctx* ctx, int n_terms, const int* sites, const int* offsets, const int* counts,
+                      int n_entries, const int* out_index, const double* values);
+
+/*
+ * Sets up B independent chains: configs[b*L1*L2 + l1*L2 + l2] are physical indices, seeds[b]
+ * seeds chain b's mt19937_64 exactly as TAT.random.seed does, and `discard` uniform_real draws
+ * are skipped first (SeedDiffer draws one, tetragono/tetragono/utility.py:146-150).
+ * Replaces: Configuration.import_configuration (lattice.py:181-206) + TAT.random.seed (PyTAT/PyTAT.hpp:89-94).
+ */
+int tnsp_chains_init(tnsp_ctx* ctx, int B, const int32_t* configs, const uint64_t* seeds, int discard,
+                     int precision);
+
+/*
+ * Runs `nsweeps` sweeps of every chain.  When `observe` is non-zero every sweep is followed by
+ * the observation of its configuration: E_loc, the gradient holes and the reweighted
+ * accumulators (energy, Delta, E*Delta), and per-sample E_loc and log|ws| are recorded.
+ * Replaces: SweepSampling.__call__ (sampling.py:145-154, with _single_term :117-143) and
+ * Observer.__call__ (tetragono/tetragono/sampling_lattice/observer.py:313-415).
+ */
+int tnsp_sweep(tnsp_ctx* ctx, int nsweeps, int observe);
+
+/* Zeroes the observer accumulators and the per-sample record (Observer.__enter__, observer.py:41-81). */
+int tnsp_observer_reset(tnsp_ctx* ctx);
+
+/*
+ * Reads the reduced accumulators (Observer.__exit__ + estimators, observer.py:83-126, 433-555):
+ * scalars[0..7] = count, total_weight, total_weight_square, total_log_ws, sum E*w, sum E*w^2,
+ * sum E^2*w^2, number of proposals accepted; delta / edelta (may be NULL) receive sum hole*w and
+ * sum E*hole*w in the dense site layout of tnsp_lattice_upload.
+ */
+int tnsp_observer_read(tnsp_ctx* ctx, double* scalars, double* delta, double* edelta);
+
+/*
+ * Copies the per-sample record of the last tnsp_sweep(observe=1) call: eloc[s*B + b],
+ * log_ws[s*B + b] (natural log of |ws|) and reweight[s*B + b] for s < nsweeps.
+ */
+int tnsp_samples_read(tnsp_ctx* ctx, double* eloc, double* log_ws, double* reweight);
+
+/* Copies the chains' current configurations (export_configuration, lattice.py:208-229) and, if
+ * not NULL, the sampling weight log|ws|^2 of their last sweep (log of `possibility`). */
+int tnsp_chains_read(tnsp_ctx* ctx, int32_t* configs, double* log_possibility);
+
+/*
+ * Amplitude ws = hole(()) of B arbitrary configurations (row-0 strip of the truncated boundary
+ * MPS, tetragono/tetragono/auxiliaries/single_layer_auxiliaries.py:710-720); results as
+ * mantissa * 2^exponent.
+ */
+int tnsp_amplitude(tnsp_ctx* ctx, int B, const int32_t* configs, double* mantissa, int32_t* exponent);
+
+/* Returns and clears the device status word (TNSP_ST_* bits). */
+int tnsp_device_status(tnsp_ctx* ctx, int32_t* status);
+
+/* Milliseconds spent in the last tnsp_sweep's kernels (CUDA events on the context stream), and the
+ * number of kernel launches it made. */
+int tnsp_last_timing(tnsp_ctx* ctx, double* ms, int64_t* launches);
+
+/*
+ * Algorithmic work done by tnsp_sweep since the last reset, in floating-point operations:
+ * flops[0] block contractions (2mnk per product), flops[1] Householder QR (with explicit Q),
+ * flops[2] truncated SVD (Golub-Van Loan count 4m^2n + 8mn^2 + 9n^3), flops[3] strip
+ * environments and holes.  `reset` non-zero zeroes the counters after reading.
+ * No reference counterpart: instrumentation for the roofline of the sampler kernel.
+ */
+int tnsp_counters_read(tnsp_ctx* ctx, double* flops, int reset);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

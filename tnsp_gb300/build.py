@@ -1,0 +1,47 @@
+"""In-tree build of the CUDA library for GB300 (sm_103a)."""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "libtnsp_gb300.so")
+SOURCES = [os.path.join(CSRC, "tnsp_capi.cu")]
+DEPS = SOURCES + [os.path.join(CSRC, f) for f in ("sampler.cu", "cta_linalg.cuh")] + [
+    os.path.join(os.path.dirname(HERE), "include", "tnsp_gb300.h")
+]
+NVCC_FLAGS = [
+    "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+    "-shared", "-cudart", "shared"
+]
+
+
+def nvcc():
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.sep not in cand or os.path.exists(cand)):
+            return cand
+    return "nvcc"
+
+
+def up_to_date():
+    if not os.path.exists(OUT):
+        return False
+    t = os.path.getmtime(OUT)
+    return all(os.path.getmtime(p) <= t for p in DEPS if os.path.exists(p))
+
+
+def build(force=False, verbose=False):
+    """Compiles libtnsp_gb300.so next to this file unless it is newer than its sources."""
+    if not force and up_to_date():
+        return OUT
+    cmd = [nvcc()] + NVCC_FLAGS + ["-o", OUT + ".tmp"] + SOURCES
+    if verbose:
+        print(" ".join(cmd), file=sys.stderr)
+    subprocess.run(cmd, check=True)
+    os.replace(OUT + ".tmp", OUT)
+    return OUT
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv, verbose=True)
+    print(OUT)

@@ -1,0 +1,270 @@
+// CTA-cooperative dense linear algebra for one Markov chain per thread block.
+//
+// Every routine here is called by all threads of the block with identical arguments and ends
+// with a __syncthreads(); operands live in global memory (this block's scratch slot) and are
+// row-major unless stated.  The element type T is double (the FP64 sampler) or float (the
+// mixed sampler); reductions that decide control flow are done in the element type.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace tnsp {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+
+template <class T> struct Eps;
+template <> struct Eps<double> {
+  static __device__ __forceinline__ double value() { return 1.1102230246251565e-16; }
+};
+template <> struct Eps<float> {
+  static __device__ __forceinline__ float value() { return 5.9604645e-08f; }
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+template <class T> __device__ __forceinline__ T warp_max(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Block-wide sum; `red` is shared scratch of kWarps doubles.  Result broadcast to all threads.
+template <class T> __device__ T block_sum(T v, T* red) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  T r = 0;
+#pragma unroll
+  for (int i = 0; i < kWarps; ++i) r += red[i];
+  __syncthreads();
+  return r;
+}
+
+template <class T> __device__ T block_max(T v, T* red) {
+  v = warp_max(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  T r = 0;
+#pragma unroll
+  for (int i = 0; i < kWarps; ++i) r = fmax(r, red[i]);
+  __syncthreads();
+  return r;
+}
+
+// Rescales x[0..n) by a power of two so that max|x| lies in [0.5, 1); returns the exponent e with
+// x_old = x_new * 2^e (exact: a power-of-two scaling never rounds).  All-zero input: e = 0.
+template <class T> __device__ int block_normalize(T* x, long n, T* red) {
+  T m = 0;
+  for (long i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, fabs(x[i]));
+  m = block_max(m, red);
+  if (!(m > 0) || !isfinite(m)) return 0;
+  int e;
+  frexp((double)m, &e);
+  const T s = (T)ldexp(1.0, -e);
+  for (long i = threadIdx.x; i < n; i += blockDim.x) x[i] *= s;
+  __syncthreads();
+  return e;
+}
+
+// C[m x n] = A[m x k] * B[k x n]; A has row stride lda, B row stride ldb, C row stride ldc.
+// Each thread owns a 2x2 register tile of C.
+template <class T>
+__device__ void block_gemm(int m, int n, int k, const T* __restrict__ A, int lda, const T* __restrict__ B, int ldb,
+                           T* __restrict__ C, int ldc) {
+  const int tm = (m + 1) >> 1, tn = (n + 1) >> 1;
+  const long tiles = (long)tm * tn;
+  for (long t = threadIdx.x; t < tiles; t += blockDim.x) {
+    const int i0 = (int)(t / tn) * 2, j0 = (int)(t % tn) * 2;
+    const bool i1ok = i0 + 1 < m, j1ok = j0 + 1 < n;
+    T c00 = 0, c01 = 0, c10 = 0, c11 = 0;
+    const T* a0 = A + (long)i0 * lda;
+    const T* a1 = A + (long)(i1ok ? i0 + 1 : i0) * lda;
+    for (int p = 0; p < k; ++p) {
+      const T* b = B + (long)p * ldb;
+      const T b0 = b[j0], b1 = j1ok ? b[j0 + 1] : (T)0;
+      const T x0 = a0[p], x1 = a1[p];
+      c00 = fma(x0, b0, c00);
+      c01 = fma(x0, b1, c01);
+      c10 = fma(x1, b0, c10);
+      c11 = fma(x1, b1, c11);
+    }
+    C[(long)i0 * ldc + j0] = c00;
+    if (j1ok) C[(long)i0 * ldc + j0 + 1] = c01;
+    if (i1ok) {
+      C[(long)(i0 + 1) * ldc + j0] = c10;
+      if (j1ok) C[(long)(i0 + 1) * ldc + j0 + 1] = c11;
+    }
+  }
+  __syncthreads();
+}
+
+// Householder QR of the row-major m x n matrix M (overwritten).  Writes Q (m x kk, row-major,
+// kk = min(m, n)) to Q and R (kk x n, row-major) to R.  tau: kk scratch values.
+// Reflector j: H_j = I - tau_j v v^T, v_j = 1, v below the diagonal stored in column j of M
+// (the LAPACK dgeqrf convention; any orthogonal gauge is acceptable to the callers).
+template <class T>
+__device__ void block_qr(int m, int n, T* M, T* Q, T* R, T* tau, T* red) {
+  const int kk = m < n ? m : n;
+  __shared__ T s_beta, s_tau, s_scale;
+  for (int j = 0; j < kk; ++j) {
+    // norm of M[j+1:m, j]
+    T part = 0;
+    for (int r = j + 1 + threadIdx.x; r < m; r += blockDim.x) {
+      const T x = M[(long)r * n + j];
+      part = fma(x, x, part);
+    }
+    const T sigma = block_sum(part, red);
+    if (threadIdx.x == 0) {
+      const T alpha = M[(long)j * n + j];
+      if (sigma == (T)0) {
+        s_tau = 0;
+        s_beta = alpha;
+        s_scale = 0;
+      } else {
+        T beta = sqrt(alpha * alpha + sigma);
+        if (alpha > 0) beta = -beta;
+        s_tau = (beta - alpha) / beta;
+        s_scale = (T)1 / (alpha - beta);
+        s_beta = beta;
+      }
+      tau[j] = s_tau;
+    }
+    __syncthreads();
+    const T tj = s_tau, sc = s_scale;
+    if (tj != (T)0) {
+      for (int r = j + 1 + threadIdx.x; r < m; r += blockDim.x) M[(long)r * n + j] *= sc;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) M[(long)j * n + j] = s_beta;
+    // apply H_j to columns j+1..n-1: warp per column
+    if (tj != (T)0) {
+      const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+      for (int c = j + 1 + w; c < n; c += kWarps) {
+        T d = lane == 0 ? M[(long)j * n + c] : (T)0;
+        for (int r = j + 1 + lane; r < m; r += 32) d = fma(M[(long)r * n + j], M[(long)r * n + c], d);
+        d = warp_sum(d) * tj;
+        if (lane == 0) M[(long)j * n + c] -= d;
+        for (int r = j + 1 + lane; r < m; r += 32) M[(long)r * n + c] -= d * M[(long)r * n + j];
+      }
+    }
+    __syncthreads();
+  }
+  // R = upper triangle of the first kk rows
+  for (long t = threadIdx.x; t < (long)kk * n; t += blockDim.x) {
+    const int i = (int)(t / n), c = (int)(t % n);
+    R[t] = c >= i ? M[(long)i * n + c] : (T)0;
+  }
+  // Q = H_0 ... H_{kk-1} [I; 0], accumulated backwards
+  for (long t = threadIdx.x; t < (long)m * kk; t += blockDim.x) {
+    const int i = (int)(t / kk), c = (int)(t % kk);
+    Q[t] = i == c ? (T)1 : (T)0;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int j = kk - 1; j >= 0; --j) {
+    const T tj = tau[j];
+    if (tj != (T)0) {
+      for (int c = j + w; c < kk; c += kWarps) {
+        T d = lane == 0 ? Q[(long)j * kk + c] : (T)0;
+        for (int r = j + 1 + lane; r < m; r += 32) d = fma(M[(long)r * n + j], Q[(long)r * kk + c], d);
+        d = warp_sum(d) * tj;
+        if (lane == 0) Q[(long)j * kk + c] -= d;
+        for (int r = j + 1 + lane; r < m; r += 32) Q[(long)r * kk + c] -= d * M[(long)r * n + j];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// One-sided (Hestenes) Jacobi on nv vectors X[j][0..len) (vector-major), accumulating the same
+// rotations into Vr[j][0..nv) (initialised to the identity here).  Pairs are visited in the
+// round-robin (circle) order, one warp per pair.  Returns the number of sweeps, or -1 if the
+// sweep limit was reached without convergence.
+template <class T>
+__device__ int block_jacobi(int nv, int len, T* X, T* Vr, int max_sweeps) {
+  __shared__ int s_rot;
+  for (long t = threadIdx.x; t < (long)nv * nv; t += blockDim.x) Vr[t] = (t / nv == t % nv) ? (T)1 : (T)0;
+  __syncthreads();
+  if (nv < 2) return 0;
+  const int np = nv + (nv & 1);  // padded to even; index nv is a dummy
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  // Relative orthogonality target eps*len.  A vector whose squared norm is below
+  // (eps*len)^2 * max_j |x_j|^2 is rounding noise (a numerically zero singular value, which the
+  // callers discard); pairs involving one are not rotated, which keeps graded noise-vs-signal
+  // pairs from oscillating at the tolerance.
+  const T tol = Eps<T>::value() * (T)len;
+  __shared__ T s_red[kWarps];
+  for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+    T mx = 0;
+    for (int j = w; j < nv; j += kWarps) {
+      T a = 0;
+      for (int r = lane; r < len; r += 32) a = fma(X[(long)j * len + r], X[(long)j * len + r], a);
+      mx = fmax(mx, warp_sum(a));
+    }
+    mx = block_max(mx, s_red);
+    const T noise2 = mx * tol * tol;
+    if (threadIdx.x == 0) s_rot = 0;
+    __syncthreads();
+    int rot = 0;
+    for (int round = 0; round < np - 1; ++round) {
+      for (int k = w; k < np / 2; k += kWarps) {
+        const int i = k == 0 ? 0 : ((k + round - 1) % (np - 1)) + 1;
+        const int j = ((np - 1 - k + round - 1) % (np - 1)) + 1;
+        if (i >= nv || j >= nv) continue;
+        T* xi = X + (long)i * len;
+        T* xj = X + (long)j * len;
+        T a = 0, b = 0, g = 0;
+        for (int r = lane; r < len; r += 32) {
+          const T u = xi[r], v = xj[r];
+          a = fma(u, u, a);
+          b = fma(v, v, b);
+          g = fma(u, v, g);
+        }
+        a = warp_sum(a);
+        b = warp_sum(b);
+        g = warp_sum(g);
+        if (a <= noise2 || b <= noise2) continue;
+        if (!(fabs(g) > tol * sqrt(a) * sqrt(b))) continue;
+        rot = 1;
+        const T zeta = (b - a) / ((T)2 * g);
+        const T t = (zeta >= 0 ? (T)1 : (T)-1) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
+        const T c = (T)1 / sqrt((T)1 + t * t);
+        const T s = c * t;
+        for (int r = lane; r < len; r += 32) {
+          const T u = xi[r], v = xj[r];
+          xi[r] = c * u - s * v;
+          xj[r] = s * u + c * v;
+        }
+        T* vi = Vr + (long)i * nv;
+        T* vj = Vr + (long)j * nv;
+        for (int r = lane; r < nv; r += 32) {
+          const T u = vi[r], v = vj[r];
+          vi[r] = c * u - s * v;
+          vj[r] = s * u + c * v;
+        }
+      }
+      __syncthreads();
+    }
+    if (rot) s_rot = 1;  // benign race: every writer stores 1
+    __syncthreads();
+    const int any = s_rot;
+    __syncthreads();
+    if (!any) return sweep + 1;
+  }
+  return -1;
+}
+
+}  // namespace tnsp

@@ -1,0 +1,1097 @@
+// Sweep sampling, local energy and gradient holes of a PEPS on one GPU.
+//
+// One thread block owns one Markov chain at a time (persistent blocks stride over thousands of
+// chains).  Inside a block the chain's boundary MPSs, strip environments and compression
+// workspace live in the block's scratch slot in HBM; a lazily-validated cache mirrors the
+// reference's lazy DAG (lazy_graph/lazy/__init__.py, tetragono/tetragono/auxiliaries/
+// single_layer_auxiliaries.py:106-244): every cached tensor is a deterministic function of the
+// chain's current configuration, so recomputing it yields the value the reference would read.
+//
+// Reference semantics restated here (file:line in USTC-TNS/TNSP):
+//  * _two_line_to_one_line: contraction, QR sweep, truncating SVD sweep
+//      (tetragono/tetragono/auxiliaries/single_layer_auxiliaries.py:462-498)
+//  * strips, replace (two-site) and hole (single_layer_auxiliaries.py:254-312, 568-692, 710-729)
+//  * SweepSampling._single_term / __call__ (tetragono/tetragono/sampling_lattice/sampling.py:117-154)
+//  * Observer.__call__ (tetragono/tetragono/sampling_lattice/observer.py:313-415)
+//  * TAT.random: std::mt19937_64 with libstdc++'s uniform_int / uniform_real (PyTAT/PyTAT.hpp:86-113)
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "cta_linalg.cuh"
+
+namespace tnsp {
+
+constexpr int kMaxL = 16;       // lattice extent limit (rows or columns)
+constexpr int kMaxSites = kMaxL * kMaxL;
+constexpr int kMtN = 312;
+constexpr int kMaxSweepsJacobi = 60;
+
+enum { ST_SVD_NOCONV = 1, ST_NONFINITE = 2, ST_UNSUPPORTED = 4, ST_ZERO_WS = 8 };
+enum { F_UP = 0, F_DOWN = 1, F_LEFT = 2, F_RIGHT = 3 };
+
+struct Model {
+  int L1, L2, P, cut, Dmax;
+  const int* dims;          // [site][4] = U, D, L, R extents
+  const long long* off;     // [site] element offset of A[site]
+  const void* A;            // element type T, A[site][p][u][d][l][r]
+  int n_terms;
+  const int* term_sites;    // [t][4]
+  const int* hterm;         // [site]: term on (l1,l2)-(l1,l2+1) or -1
+  const int* vterm;         // [site]: term on (l1,l2)-(l1+1,l2) or -1
+  const int* hflip;         // [t]: 1 if positions[0] is the second (right/lower) site
+  const int* tab_off;       // [t][P*P]
+  const int* tab_cnt;       // [t][P*P], -1 = input absent from the table
+  const int* tab_out;       // [entries]
+  const double* tab_val;    // [entries]
+  long long n_params;       // total elements of all site tensors
+};
+
+struct Chains {
+  int B;
+  int32_t* conf;            // [B][L1*L2]
+  uint64_t* mt;             // [B][312]
+  int32_t* mti;             // [B]
+  double* ws_m;             // [B] carried amplitude of the last sweep (mantissa)
+  int32_t* ws_e;            // [B]
+  int64_t* accepted;        // [B]
+  double* acc;              // [B][8] observer scalars (see tnsp_observer_read)
+  double* rec_eloc;         // [nsamples][B]
+  double* rec_logws;
+  double* rec_rw;
+  int32_t* status;
+};
+
+struct Slots {
+  long long stride;         // elements of T per slot
+  long long o_lines[4];     // line storage per family: [line][site][capB]
+  long long capB, capT, capR, capE, capS, capH;
+  long long o_T, o_R, o_tau, o_X, o_V, o_sig, o_E, o_F, o_t1, o_t2, o_w0, o_w1, o_h;
+  int* ldims;               // [slot][4][kMaxL][kMaxL][3]
+  int* lexp;                // [slot][4][kMaxL]
+  int* order;               // [slot][cut*Dmax]
+  double* delta;            // [slot][n_params]
+  double* edelta;           // [slot][n_params]
+  double* contrib;          // [slot][n_terms]
+  double* flops;            // [slot][4]: algorithmic flops of contractions, QR, SVD, strip/hole work
+};
+
+// ------------------------------------------------------------------------------------------
+// random numbers: std::mt19937_64 + libstdc++ 13 distributions (thread 0 only)
+// ------------------------------------------------------------------------------------------
+__device__ uint64_t mt_next(uint64_t* mt, int& mti) {
+  if (mti >= kMtN) {
+    for (int i = 0; i < kMtN; ++i) {
+      const uint64_t x = (mt[i] & 0xFFFFFFFF80000000ull) | (mt[(i + 1) % kMtN] & 0x7FFFFFFFull);
+      uint64_t xa = x >> 1;
+      if (x & 1ull) xa ^= 0xB5026F5AA96619E9ull;
+      mt[i] = mt[(i + 156) % kMtN] ^ xa;
+    }
+    mti = 0;
+  }
+  uint64_t y = mt[mti++];
+  y ^= (y >> 29) & 0x5555555555555555ull;
+  y ^= (y << 17) & 0x71D67FFFEDA60000ull;
+  y ^= (y << 37) & 0xFFF7EEE000000000ull;
+  y ^= y >> 43;
+  return y;
+}
+
+// std::uniform_int_distribution<int>(0, n-1): Lemire's nearly-divisionless downscaling on a
+// 128-bit product (bits/uniform_int_dist.h, _S_nd).
+__device__ int draw_uniform_int(uint64_t* mt, int& mti, int n) {
+  const uint64_t range = (uint64_t)n;
+  uint64_t x = mt_next(mt, mti);
+  uint64_t lo = x * range;
+  uint64_t hi = __umul64hi(x, range);
+  if (lo < range) {
+    const uint64_t threshold = (0ull - range) % range;
+    while (lo < threshold) {
+      x = mt_next(mt, mti);
+      lo = x * range;
+      hi = __umul64hi(x, range);
+    }
+  }
+  return (int)hi;
+}
+
+// std::uniform_real_distribution<double>(0, 1): generate_canonical<double, 53> with one 64-bit
+// word: round-to-nearest conversion, division by 2^64, clamp to below 1.
+__device__ double draw_uniform_real(uint64_t* mt, int& mti) {
+  const uint64_t x = mt_next(mt, mti);
+  double r = __ull2double_rn(x) * 5.421010862427522e-20;  // 2^-64, exact
+  if (r >= 1.0) r = 0.99999999999999989;
+  return r;
+}
+
+// ------------------------------------------------------------------------------------------
+// views
+// ------------------------------------------------------------------------------------------
+struct SiteView {  // a projected site tensor seen as W(u, d, l, r)
+  long long base;
+  int du, dd, dl, dr;
+  int su, sd, sl, sr;
+};
+
+struct Dims3 {
+  int a, p, b;
+};
+
+template <class T> struct Chain {
+  const Model& md;
+  const Slots& sl;
+  T* slot;
+  const T* A;
+  int* ldims;
+  int* lexp;
+  int* order;
+  // shared state (pointers into shared memory)
+  short* conf;
+  unsigned char* valid;   // [4][kMaxL]
+  int* eE;                // [kMaxL + 1]
+  int* eF;
+  T* red;
+  double* dred;
+  double* fl;             // shared [4] flop counters (thread 0 adds)
+
+  __device__ void count(int k, double f) const {
+    if (threadIdx.x == 0) fl[k] += f;
+  }
+
+  __device__ T* line(int f, int idx, int i) const {
+    const int ns = (f < 2) ? md.L2 : md.L1;
+    return slot + sl.o_lines[f] + ((long long)idx * ns + i) * sl.capB;
+  }
+  __device__ int* ldim(int f, int idx, int i) const { return ldims + (((f * kMaxL) + idx) * kMaxL + i) * 3; }
+
+  // site (l1, l2) at physical index s in one of four orientations:
+  //   0: (U, D, L, R)   1: (D, U, L, R)   2: (L, R, U, D)   3: (R, L, U, D)
+  __device__ SiteView site(int l1, int l2, int s, int orient) const {
+    const int id = l1 * md.L2 + l2;
+    const int* d = md.dims + id * 4;
+    const int U = d[0], D = d[1], L = d[2], R = d[3];
+    const int sR = 1, sL = R, sD = L * R, sU = D * L * R;
+    SiteView v;
+    v.base = md.off[id] + (long long)s * U * D * L * R;
+    switch (orient) {
+      case 0: v.du = U; v.su = sU; v.dd = D; v.sd = sD; v.dl = L; v.sl = sL; v.dr = R; v.sr = sR; break;
+      case 1: v.du = D; v.su = sD; v.dd = U; v.sd = sU; v.dl = L; v.sl = sL; v.dr = R; v.sr = sR; break;
+      case 2: v.du = L; v.su = sL; v.dd = R; v.sd = sR; v.dl = U; v.sl = sU; v.dr = D; v.sr = sD; break;
+      default: v.du = R; v.su = sR; v.dd = L; v.sd = sL; v.dl = U; v.sl = sU; v.dr = D; v.sr = sD; break;
+    }
+    return v;
+  }
+};
+
+// ------------------------------------------------------------------------------------------
+// contractions
+// ------------------------------------------------------------------------------------------
+// out[(x*l + y), dd, (z*r + w)] = sum_p line[x, p, z] * W(p, dd, y, w)
+template <class T>
+__device__ void two_line(const T* __restrict__ line, Dims3 ld, const T* __restrict__ A, SiteView w, T* __restrict__ out) {
+  const int Am = ld.a * w.dl, Bm = ld.b * w.dr;
+  const long long n = (long long)Am * w.dd * Bm;
+  for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+    const int col = (int)(t % Bm);
+    const long long rest = t / Bm;
+    const int dd = (int)(rest % w.dd);
+    const int row = (int)(rest / w.dd);
+    const int x = row / w.dl, y = row % w.dl, z = col / w.dr, ww = col % w.dr;
+    T acc = 0;
+    const T* lp = line + (long long)x * ld.p * ld.b + z;
+    const T* wp = A + w.base + (long long)dd * w.sd + (long long)y * w.sl + (long long)ww * w.sr;
+    for (int p = 0; p < ld.p; ++p) acc = fma(lp[(long long)p * ld.b], wp[(long long)p * w.su], acc);
+    out[t] = acc;
+  }
+  __syncthreads();
+}
+
+// E'[a, r, b] = sum E[x, y, z] up[x, u, a] W(u, d, y, r) dn[z, d, b]
+template <class T>
+__device__ void strip_left(const T* E, int X, int Y, int Z, const T* up, Dims3 ud, const T* A, SiteView w,
+                           const T* dn, Dims3 dd, T* t1, T* t2, T* out) {
+  const int U = ud.p, Aa = ud.b, D = dd.p, Bb = dd.b, R = w.dr;
+  // t1[y, z, u, a] = sum_x E[x, y, z] up[x, u, a]
+  long long n = (long long)Y * Z * U * Aa;
+  for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+    const int a = (int)(t % Aa);
+    long long r = t / Aa;
+    const int u = (int)(r % U);
+    r /= U;
+    const int z = (int)(r % Z);
+    const int y = (int)(r / Z);
+    T acc = 0;
+    for (int x = 0; x < X; ++x) acc = fma(E[((long long)x * Y + y) * Z + z], up[((long long)x * U + u) * Aa + a], acc);
+    t1[t] = acc;
+  }
+  __syncthreads();
+  // t2[z, a, d, r] = sum_{y,u} t1[y, z, u, a] W(u, d, y, r)
+  n = (long long)Z * Aa * D * R;
+  for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+    const int rr = (int)(t % R);
+    long long q = t / R;
+    const int d = (int)(q % D);
+    q /= D;
+    const int a = (int)(q % Aa);
+    const int z = (int)(q / Aa);
+    T acc = 0;
+    for (int y = 0; y < Y; ++y)
+      for (int u = 0; u < U; ++u)
+        acc = fma(t1[(((long long)y * Z + z) * U + u) * Aa + a],
+                  A[w.base + (long long)u * w.su + (long long)d * w.sd + (long long)y * w.sl + (long long)rr * w.sr], acc);
+    t2[t] = acc;
+  }
+  __syncthreads();
+  // out[a, r, b] = sum_{z,d} t2[z, a, d, r] dn[z, d, b]
+  n = (long long)Aa * R * Bb;
+  for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+    const int b = (int)(t % Bb);
+    long long q = t / Bb;
+    const int rr = (int)(q % R);
+    const int a = (int)(q / R);
+    T acc = 0;
+    for (int z = 0; z < Z; ++z)
+      for (int d = 0; d < D; ++d)
+        acc = fma(t2[(((long long)z * Aa + a) * D + d) * R + rr], dn[((long long)z * D + d) * Bb + b], acc);
+    out[t] = acc;
+  }
+  __syncthreads();
+}
+
+// F'[x, l, z] = sum F[a, r, b] up[x, u, a] W(u, d, l, r) dn[z, d, b]
+template <class T>
+__device__ void strip_right(const T* F, int Aa, int R, int Bb, const T* up, Dims3 ud, const T* A, SiteView w,
+                            const T* dn, Dims3 dd, T* s1, T* s2, T* out) {
+  const int X = ud.a, U = ud.p, Z = dd.a, D = dd.p, L = w.dl;
+  // s1[x, u, r, b] = sum_a up[x, u, a] F[a, r, b]
+  long long n = (long long)X * U * R * Bb;
+  for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+    const int b = (int)(t % Bb);
+    long long q = t / Bb;
+    const int rr = (int)(q % R);
+    q /= R;
+    const int u = (int)(q % U);
+    const int x = (int)(q / U);
+    T acc = 0;
+    for (int a = 0; a < Aa; ++a) acc = fma(up[((long long)x * U + u) * Aa + a], F[((long long)a * R + rr) * Bb + b], acc);
+    s1[t] = acc;
+  }
+  __syncthreads();
+  // s2[x, l, d, b] = sum_{u,r} s1[x, u, r, b] W(u, d, l, r)
+  n = (long long)X * L * D * Bb;
+  for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+    const int b = (int)(t % Bb);
+    long long q = t / Bb;
+    const int d = (int)(q % D);
+    q /= D;
+    const int l = (int)(q % L);
+    const int x = (int)(q / L);
+    T acc = 0;
+    for (int u = 0; u < U; ++u)
+      for (int rr = 0; rr < R; ++rr)
+        acc = fma(s1[(((long long)x * U + u) * R + rr) * Bb + b],
+                  A[w.base + (long long)u * w.su + (long long)d * w.sd + (long long)l * w.sl + (long long)rr * w.sr], acc);
+    s2[t] = acc;
+  }
+  __syncthreads();
+  // out[x, l, z] = sum_{d,b} s2[x, l, d, b] dn[z, d, b]
+  n = (long long)X * L * Z;
+  for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+    const int z = (int)(t % Z);
+    long long q = t / Z;
+    const int l = (int)(q % L);
+    const int x = (int)(q / L);
+    T acc = 0;
+    for (int d = 0; d < D; ++d)
+      for (int b = 0; b < Bb; ++b)
+        acc = fma(s2[(((long long)x * L + l) * D + d) * Bb + b], dn[((long long)z * D + d) * Bb + b], acc);
+    out[t] = acc;
+  }
+  __syncthreads();
+}
+
+// h[u, d, l, r] = sum E[x, l, z] up[x, u, a] dn[z, d, b] F[a, r, b]
+template <class T>
+__device__ void strip_hole(const T* E, int X, int L, int Z, const T* up, Dims3 ud, const T* dn, Dims3 dd, const T* F,
+                           int R, T* h1, T* h2, T* out) {
+  const int U = ud.p, Aa = ud.b, D = dd.p, Bb = dd.b;
+  long long n = (long long)L * Z * U * Aa;
+  for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+    const int a = (int)(t % Aa);
+    long long q = t / Aa;
+    const int u = (int)(q % U);
+    q /= U;
+    const int z = (int)(q % Z);
+    const int l = (int)(q / Z);
+    T acc = 0;
+    for (int x = 0; x < X; ++x) acc = fma(E[((long long)x * L + l) * Z + z], up[((long long)x * U + u) * Aa + a], acc);
+    h1[t] = acc;
+  }
+  __syncthreads();
+  // h2[l, u, a, d, b] = sum_z h1[l, z, u, a] dn[z, d, b]
+  n = (long long)L * U * Aa * D * Bb;
+  for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+    const int b = (int)(t % Bb);
+    long long q = t / Bb;
+    const int d = (int)(q % D);
+    q /= D;
+    const int a = (int)(q % Aa);
+    q /= Aa;
+    const int u = (int)(q % U);
+    const int l = (int)(q / U);
+    T acc = 0;
+    for (int z = 0; z < Z; ++z)
+      acc = fma(h1[(((long long)l * Z + z) * U + u) * Aa + a], dn[((long long)z * D + d) * Bb + b], acc);
+    h2[t] = acc;
+  }
+  __syncthreads();
+  n = (long long)U * D * L * R;
+  for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+    const int rr = (int)(t % R);
+    long long q = t / R;
+    const int l = (int)(q % L);
+    q /= L;
+    const int d = (int)(q % D);
+    const int u = (int)(q / D);
+    T acc = 0;
+    for (int a = 0; a < Aa; ++a)
+      for (int b = 0; b < Bb; ++b)
+        acc = fma(h2[((((long long)l * U + u) * Aa + a) * D + d) * Bb + b], F[((long long)a * R + rr) * Bb + b], acc);
+    out[t] = acc;
+  }
+  __syncthreads();
+}
+
+template <class T> __device__ T block_dot(const T* x, const T* y, long long n, T* red) {
+  T acc = 0;
+  for (long long t = threadIdx.x; t < n; t += blockDim.x) acc = fma(x[t], y[t], acc);
+  return block_sum(acc, red);
+}
+
+// ------------------------------------------------------------------------------------------
+// the chain engine
+// ------------------------------------------------------------------------------------------
+template <class T> struct Engine : Chain<T> {
+  using Chain<T>::md;
+  using Chain<T>::sl;
+  using Chain<T>::slot;
+  using Chain<T>::A;
+  using Chain<T>::conf;
+  using Chain<T>::valid;
+  using Chain<T>::eE;
+  using Chain<T>::eF;
+  using Chain<T>::red;
+  using Chain<T>::line;
+  using Chain<T>::ldim;
+  using Chain<T>::site;
+  using Chain<T>::lexp;
+  using Chain<T>::order;
+  const T* ones;
+  int32_t* status;
+  // strip currently held in E/F: kind 0 = row, 1 = column, -1 none
+  int* strip_kind;
+  int* strip_idx;
+  int* strip_eupto;       // E[0..eupto] valid
+  int* strip_ffrom;       // F[ffrom..n] valid
+
+  __device__ int nsites_along(int f) const { return f < 2 ? md.L2 : md.L1; }
+  __device__ int nlines(int f) const { return f < 2 ? md.L1 : md.L2; }
+
+  // line family f at index idx, or the all-ones line beyond the lattice edge
+  __device__ bool is_ones(int f, int idx) const { return idx < 0 || idx >= nlines(f); }
+  __device__ const T* lsite(int f, int idx, int i) const { return is_ones(f, idx) ? ones : line(f, idx, i); }
+  __device__ Dims3 lsdim(int f, int idx, int i) const {
+    if (is_ones(f, idx)) return Dims3{1, 1, 1};
+    const int* d = ldim(f, idx, i);
+    return Dims3{d[0], d[1], d[2]};
+  }
+  __device__ int lexpo(int f, int idx) const { return is_ones(f, idx) ? 0 : lexp[f * kMaxL + idx]; }
+
+  __device__ T* Tbuf(int k) const { return slot + sl.o_T + (long long)k * sl.capT; }
+
+  // _two_line_to_one_line for family f producing line idx (single_layer_auxiliaries.py:462-498)
+  __device__ void compress(int f, int idx) {
+    const int n = nsites_along(f);
+    const int prev = (f == F_UP || f == F_LEFT) ? idx - 1 : idx + 1;
+    const int orient = f;  // 0: UDLR, 1: DULR, 2: LRUD, 3: RLUD
+    __shared__ int s_buf[kMaxL + 2];
+    __shared__ int s_dA[kMaxL], s_dd[kMaxL], s_dB[kMaxL];
+    // slot buffers: T pool has n + 2 buffers; s_buf maps site -> buffer
+    if (threadIdx.x < n + 2) s_buf[threadIdx.x] = threadIdx.x;
+    __syncthreads();
+    int expo = lexpo(f, prev);
+    for (int i = 0; i < n; ++i) {
+      const int l1 = (f < 2) ? idx : i, l2 = (f < 2) ? i : idx;
+      const SiteView w = site(l1, l2, conf[l1 * md.L2 + l2], orient);
+      const Dims3 ld = lsdim(f, prev, i);
+      two_line(lsite(f, prev, i), ld, A, w, Tbuf(s_buf[i]));
+      this->count(0, 2.0 * ld.a * w.dl * w.dd * ld.b * w.dr * ld.p);
+      if (threadIdx.x == 0) {
+        s_dA[i] = ld.a * w.dl;
+        s_dd[i] = w.dd;
+        s_dB[i] = ld.b * w.dr;
+      }
+      __syncthreads();
+    }
+    T* R = slot + sl.o_R;
+    T* tau = slot + sl.o_tau;
+    // QR sweep
+    for (int i = 0; i < n - 1; ++i) {
+      const int rows = s_dA[i] * s_dd[i], cols = s_dB[i];
+      const int kk = rows < cols ? rows : cols;
+      const int spare = s_buf[n];
+      block_qr(rows, cols, Tbuf(s_buf[i]), Tbuf(spare), R, tau, red);
+      {
+        const double mm = rows > cols ? rows : cols, nn = kk;
+        this->count(1, 2.0 * (2.0 * mm * nn * nn - 2.0 * nn * nn * nn / 3.0));
+      }
+      if (threadIdx.x == 0) {
+        s_buf[n] = s_buf[i];
+        s_buf[i] = spare;
+        s_dB[i] = kk;
+      }
+      __syncthreads();
+      // T[i+1] <- R * T[i+1]
+      const int spare2 = s_buf[n];
+      block_gemm(kk, s_dd[i + 1] * s_dB[i + 1], cols, R, cols, Tbuf(s_buf[i + 1]), s_dd[i + 1] * s_dB[i + 1],
+                 Tbuf(spare2), s_dd[i + 1] * s_dB[i + 1]);
+      this->count(0, 2.0 * kk * cols * s_dd[i + 1] * s_dB[i + 1]);
+      if (threadIdx.x == 0) {
+        s_buf[n] = s_buf[i + 1];
+        s_buf[i + 1] = spare2;
+        s_dA[i + 1] = kk;
+      }
+      __syncthreads();
+      expo += block_normalize(Tbuf(s_buf[i + 1]), (long long)kk * s_dd[i + 1] * s_dB[i + 1], red);
+    }
+    // SVD sweep with truncation
+    T* X = slot + sl.o_X;
+    T* V = slot + sl.o_V;
+    T* sig = slot + sl.o_sig;
+    for (int i = n - 1; i >= 1; --i) {
+      const int rows = s_dA[i], cols = s_dd[i] * s_dB[i];
+      const T* M = Tbuf(s_buf[i]);
+      const bool caseA = cols <= rows;
+      const int nv = caseA ? cols : rows, len = caseA ? rows : cols;
+      if (caseA) {
+        for (long long t = threadIdx.x; t < (long long)nv * len; t += blockDim.x) {
+          const int j = (int)(t / len), r = (int)(t % len);
+          X[t] = M[(long long)r * cols + j];
+        }
+      } else {
+        for (long long t = threadIdx.x; t < (long long)nv * len; t += blockDim.x) X[t] = M[t];
+      }
+      __syncthreads();
+      const int sweeps = block_jacobi(nv, len, X, V, kMaxSweepsJacobi);
+      {
+        const double mm = len, nn = nv;
+        this->count(2, 4.0 * mm * mm * nn + 8.0 * mm * nn * nn + 9.0 * nn * nn * nn);
+      }
+      if (sweeps < 0 && threadIdx.x == 0) atomicOr(status, ST_SVD_NOCONV);
+      // singular values
+      {
+        const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+        for (int j = wp; j < nv; j += kWarps) {
+          T s2 = 0;
+          for (int r = lane; r < len; r += 32) s2 = fma(X[(long long)j * len + r], X[(long long)j * len + r], s2);
+          s2 = warp_sum(s2);
+          if (lane == 0) sig[j] = sqrt(s2);
+        }
+      }
+      __syncthreads();
+      const int c = md.cut < nv ? md.cut : nv;
+      // rank selection: descending, ties by index
+      for (int j = threadIdx.x; j < nv; j += blockDim.x) {
+        const T sj = sig[j];
+        int rank = 0;
+        for (int k = 0; k < nv; ++k) {
+          const T sk = sig[k];
+          rank += (sk > sj) || (sk == sj && k < j);
+        }
+        if (rank < c) order[rank] = j;
+      }
+      __syncthreads();
+      T smax = 0;
+      for (int j = threadIdx.x; j < nv; j += blockDim.x) smax = fmax(smax, sig[j]);
+      smax = block_max(smax, red);
+      const T thr = smax * Eps<T>::value() * (T)len;
+      // new T[i] (c x cols) into spare, US (rows x c) into R
+      const int spare = s_buf[n];
+      T* Tn = Tbuf(spare);
+      for (long long t = threadIdx.x; t < (long long)c * cols; t += blockDim.x) {
+        const int tr = (int)(t / cols), q = (int)(t % cols);
+        const int j = order[tr];
+        T v;
+        if (caseA) {
+          v = V[(long long)j * nv + q];
+        } else {
+          const T s = sig[j];
+          v = s > thr ? X[(long long)j * len + q] / s : (T)0;
+        }
+        Tn[t] = v;
+      }
+      for (long long t = threadIdx.x; t < (long long)rows * c; t += blockDim.x) {
+        const int r = (int)(t / c), tr = (int)(t % c);
+        const int j = order[tr];
+        T v;
+        if (caseA) {
+          v = X[(long long)j * len + r];
+        } else {
+          const T s = sig[j];
+          v = s > thr ? V[(long long)j * nv + r] * s : (T)0;
+        }
+        R[t] = v;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        s_buf[n] = s_buf[i];
+        s_buf[i] = spare;
+        s_dA[i] = c;
+      }
+      __syncthreads();
+      // T[i-1] <- T[i-1] * US
+      const int spare2 = s_buf[n];
+      block_gemm(s_dA[i - 1] * s_dd[i - 1], c, rows, Tbuf(s_buf[i - 1]), rows, R, c, Tbuf(spare2), c);
+      this->count(0, 2.0 * s_dA[i - 1] * s_dd[i - 1] * rows * c);
+      if (threadIdx.x == 0) {
+        s_buf[n] = s_buf[i - 1];
+        s_buf[i - 1] = spare2;
+        s_dB[i - 1] = c;
+      }
+      __syncthreads();
+      expo += block_normalize(Tbuf(s_buf[i - 1]), (long long)s_dA[i - 1] * s_dd[i - 1] * c, red);
+    }
+    if (n == 1) expo += block_normalize(Tbuf(s_buf[0]), (long long)s_dA[0] * s_dd[0] * s_dB[0], red);
+    // store the line
+    for (int i = 0; i < n; ++i) {
+      const long long cnt = (long long)s_dA[i] * s_dd[i] * s_dB[i];
+      const T* src = Tbuf(s_buf[i]);
+      T* dst = line(f, idx, i);
+      for (long long t = threadIdx.x; t < cnt; t += blockDim.x) dst[t] = src[t];
+      if (threadIdx.x == 0) {
+        int* d = ldim(f, idx, i);
+        d[0] = s_dA[i];
+        d[1] = s_dd[i];
+        d[2] = s_dB[i];
+      }
+    }
+    if (threadIdx.x == 0) lexp[f * kMaxL + idx] = expo;
+    __syncthreads();
+  }
+
+  // make line (f, idx) valid for the current configuration (recomputing its invalid upstreams)
+  __device__ void ensure(int f, int idx) {
+    if (is_ones(f, idx)) return;
+    const bool forward = (f == F_UP || f == F_LEFT);
+    if (valid[f * kMaxL + idx]) return;
+    // first invalid index in the dependency chain
+    int start = idx;
+    if (forward) {
+      while (start - 1 >= 0 && !valid[f * kMaxL + start - 1]) --start;
+      for (int k = start; k <= idx; ++k) {
+        compress(f, k);
+        if (threadIdx.x == 0) valid[f * kMaxL + k] = 1;
+        __syncthreads();
+      }
+    } else {
+      while (start + 1 < nlines(f) && !valid[f * kMaxL + start + 1]) ++start;
+      for (int k = start; k >= idx; --k) {
+        compress(f, k);
+        if (threadIdx.x == 0) valid[f * kMaxL + k] = 1;
+        __syncthreads();
+      }
+    }
+  }
+
+  // sites changed: invalidate every line that contains them and the strip cache
+  __device__ void invalidate_site(int l1, int l2) {
+    if (threadIdx.x == 0) {
+      for (int k = l1; k < md.L1; ++k) valid[F_UP * kMaxL + k] = 0;
+      for (int k = 0; k <= l1; ++k) valid[F_DOWN * kMaxL + k] = 0;
+      for (int k = l2; k < md.L2; ++k) valid[F_LEFT * kMaxL + k] = 0;
+      for (int k = 0; k <= l2; ++k) valid[F_RIGHT * kMaxL + k] = 0;
+    }
+  }
+
+  // strip geometry: kind 0 = row idx (lines up/down, orientation 0), 1 = column idx (left/right, orientation 2)
+  __device__ int strip_len(int kind) const { return kind == 0 ? md.L2 : md.L1; }
+  __device__ void strip_site_rc(int kind, int idx, int c, int& l1, int& l2) const {
+    if (kind == 0) { l1 = idx; l2 = c; } else { l1 = c; l2 = idx; }
+  }
+  __device__ int fup(int kind) const { return kind == 0 ? F_UP : F_LEFT; }
+  __device__ int fdn(int kind) const { return kind == 0 ? F_DOWN : F_RIGHT; }
+
+  __device__ T* Ebuf(int c) const { return slot + sl.o_E + (long long)c * sl.capE; }
+  __device__ T* Fbuf(int c) const { return slot + sl.o_F + (long long)c * sl.capE; }
+  __device__ Dims3 Edims(int kind, int idx, int c) const {
+    // E[c] = columns 0..c-1 : (up bond, site bond, down bond) at cut c
+    if (c == 0) return Dims3{1, 1, 1};
+    int l1, l2;
+    strip_site_rc(kind, idx, c - 1, l1, l2);
+    const SiteView w = site(l1, l2, 0, kind == 0 ? 0 : 2);
+    return Dims3{lsdim(fup(kind), idx - 1, c - 1).b, w.dr, lsdim(fdn(kind), idx + 1, c - 1).b};
+  }
+  __device__ Dims3 Fdims(int kind, int idx, int c) const {
+    const int n = strip_len(kind);
+    if (c == n) return Dims3{1, 1, 1};
+    int l1, l2;
+    strip_site_rc(kind, idx, c, l1, l2);
+    const SiteView w = site(l1, l2, 0, kind == 0 ? 0 : 2);
+    return Dims3{lsdim(fup(kind), idx - 1, c).a, w.dl, lsdim(fdn(kind), idx + 1, c).a};
+  }
+
+  // E[c+1] = E[c] x column c (physical index s); writes into dst with exponent returned
+  __device__ int step_left(int kind, int idx, int c, const T* Ein, Dims3 e, int s, T* dst) {
+    int l1, l2;
+    strip_site_rc(kind, idx, c, l1, l2);
+    const SiteView w = site(l1, l2, s, kind == 0 ? 0 : 2);
+    strip_left(Ein, e.a, e.p, e.b, lsite(fup(kind), idx - 1, c), lsdim(fup(kind), idx - 1, c), A, w,
+               lsite(fdn(kind), idx + 1, c), lsdim(fdn(kind), idx + 1, c), slot + sl.o_t1, slot + sl.o_t2, dst);
+    const Dims3 up = lsdim(fup(kind), idx - 1, c), dn = lsdim(fdn(kind), idx + 1, c);
+    this->count(3, 2.0 * ((double)e.a * e.p * e.b * up.p * up.b + (double)e.b * up.b * dn.p * w.dr * e.p * up.p +
+                          (double)up.b * w.dr * dn.b * e.b * dn.p));
+    return block_normalize(dst, (long long)up.b * w.dr * dn.b, red);
+  }
+  __device__ int step_right(int kind, int idx, int c, const T* Fin, Dims3 f, int s, T* dst) {
+    int l1, l2;
+    strip_site_rc(kind, idx, c, l1, l2);
+    const SiteView w = site(l1, l2, s, kind == 0 ? 0 : 2);
+    strip_right(Fin, f.a, f.p, f.b, lsite(fup(kind), idx - 1, c), lsdim(fup(kind), idx - 1, c), A, w,
+                lsite(fdn(kind), idx + 1, c), lsdim(fdn(kind), idx + 1, c), slot + sl.o_t1, slot + sl.o_t2, dst);
+    const Dims3 up = lsdim(fup(kind), idx - 1, c), dn = lsdim(fdn(kind), idx + 1, c);
+    this->count(3, 2.0 * ((double)up.a * up.p * f.a * f.p * f.b + (double)up.a * w.dl * dn.p * f.b * up.p * f.p +
+                          (double)up.a * w.dl * dn.a * dn.p * f.b));
+    return block_normalize(dst, (long long)up.a * w.dl * dn.a, red);
+  }
+
+  __device__ int conf_at(int kind, int idx, int c) const {
+    int l1, l2;
+    strip_site_rc(kind, idx, c, l1, l2);
+    return conf[l1 * md.L2 + l2];
+  }
+
+  // build the strip (kind, idx) for the current configuration: all F, E[0]
+  __device__ void strip_begin(int kind, int idx) {
+    ensure(fup(kind), idx - 1);
+    ensure(fdn(kind), idx + 1);
+    const int n = strip_len(kind);
+    T* F = Fbuf(n);
+    if (threadIdx.x == 0) F[0] = (T)1;
+    T* E = Ebuf(0);
+    if (threadIdx.x == 0) E[0] = (T)1;
+    if (threadIdx.x == 0) {
+      eF[n] = 0;
+      eE[0] = 0;
+    }
+    __syncthreads();
+    for (int c = n - 1; c >= 0; --c) {
+      const int e = step_right(kind, idx, c, Fbuf(c + 1), Fdims(kind, idx, c + 1), conf_at(kind, idx, c), Fbuf(c));
+      if (threadIdx.x == 0) eF[c] = eF[c + 1] + e;
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      *strip_kind = kind;
+      *strip_idx = idx;
+      *strip_eupto = 0;
+      *strip_ffrom = 0;
+    }
+    __syncthreads();
+  }
+
+  __device__ void strip_advance(int kind, int idx, int c) {
+    // make E[c] valid
+    while (*strip_eupto < c) {
+      const int k = *strip_eupto;
+      const int e = step_left(kind, idx, k, Ebuf(k), Edims(kind, idx, k), conf_at(kind, idx, k), Ebuf(k + 1));
+      if (threadIdx.x == 0) {
+        eE[k + 1] = eE[k] + e;
+        *strip_eupto = k + 1;
+      }
+      __syncthreads();
+    }
+  }
+
+  // amplitude with columns c, c+1 of the strip set to s0, s1 (E[c] and F[c+2] valid)
+  __device__ void strip_replace2(int kind, int idx, int c, int s0, int s1, double& m, int& ex) {
+    T* w0 = slot + sl.o_w0;
+    T* w1 = slot + sl.o_w1;
+    const int e0 = step_left(kind, idx, c, Ebuf(c), Edims(kind, idx, c), s0, w0);
+    const int e1 = step_left(kind, idx, c + 1, w0, Edims(kind, idx, c + 1), s1, w1);
+    const Dims3 fd = Fdims(kind, idx, c + 2);
+    const T v = block_dot(w1, Fbuf(c + 2), (long long)fd.a * fd.p * fd.b, red);
+    m = (double)v;
+    ex = eE[c] + e0 + e1 + eF[c + 2] + lexpo(fup(kind), idx - 1) + lexpo(fdn(kind), idx + 1);
+  }
+
+  // hole(()) = _inline_right_to_left[0, 0]: the row-0 strip (single_layer_auxiliaries.py:710-720)
+  __device__ void hole0(double& m, int& ex) {
+    ensure(F_DOWN, 1);
+    const int n = md.L2;
+    T* f0 = slot + sl.o_w0;
+    T* f1 = slot + sl.o_w1;
+    if (threadIdx.x == 0) f0[0] = (T)1;
+    __syncthreads();
+    int e = 0;
+    Dims3 fd{1, 1, 1};
+    for (int c = n - 1; c >= 0; --c) {
+      e += step_right(0, 0, c, f0, fd, conf_at(0, 0, c), f1);
+      fd = Fdims(0, 0, c);
+      T* t = f0;
+      f0 = f1;
+      f1 = t;
+    }
+    m = (double)f0[0];
+    ex = e + lexpo(F_DOWN, 1);
+    __syncthreads();
+  }
+};
+
+__device__ __forceinline__ double ratio_of(double m1, int e1, double m0, int e0) {
+  return ldexp(m1 / m0, e1 - e0);
+}
+
+// one Metropolis proposal on the term at (kind, idx, c)-(kind, idx, c+1)
+template <class T>
+__device__ void single_term(Engine<T>& eng, const Model& md, int kind, int idx, int c, int t, uint64_t* mt, int* s_mti,
+                            double* s_ws_m, int* s_ws_e, int* s_h0_valid, double* s_h0_m, int* s_h0_e, int64_t* accepted) {
+  __shared__ int s_sel, s_nn, s_acc, s_skip;
+  __shared__ double s_m;
+  __shared__ int s_e;
+  const int P = md.P;
+  int l1a, l2a, l1b, l2b;
+  eng.strip_site_rc(kind, idx, c, l1a, l2a);
+  eng.strip_site_rc(kind, idx, c + 1, l1b, l2b);
+  const int flip = md.hflip[t];
+  const int sa = eng.conf[l1a * md.L2 + l2a], sb = eng.conf[l1b * md.L2 + l2b];
+  const int in0 = flip ? sb : sa, in1 = flip ? sa : sb;
+  const int key = in0 * P + in1;
+  const int cnt = md.tab_cnt[t * P * P + key];
+  if (cnt <= 0) return;  // not in the element pool, or no hopping
+  if (threadIdx.x == 0) {
+    int mti = *s_mti;
+    const int pick = draw_uniform_int(mt, mti, cnt);
+    *s_mti = mti;
+    const int out = md.tab_out[md.tab_off[t * P * P + key] + pick];
+    s_sel = out;
+    s_nn = md.tab_cnt[t * P * P + out];
+  }
+  __syncthreads();
+  const int out = s_sel;
+  const int o0 = out / P, o1 = out % P;
+  const int na = flip ? o1 : o0, nb = flip ? o0 : o1;
+  double m;
+  int ex;
+  if (na == sa && nb == sb) {
+    // replace({}) returns hole(()) (single_layer_auxiliaries.py:501-509)
+    if (!*s_h0_valid) {
+      eng.hole0(m, ex);
+      if (threadIdx.x == 0) {
+        *s_h0_m = m;
+        *s_h0_e = ex;
+        *s_h0_valid = 1;
+      }
+      __syncthreads();
+    }
+    m = *s_h0_m;
+    ex = *s_h0_e;
+  } else if (na != sa && nb != sb) {
+    eng.strip_advance(kind, idx, c);
+    eng.strip_replace2(kind, idx, c, na, nb, m, ex);
+  } else {
+    if (threadIdx.x == 0) atomicOr(eng.status, ST_UNSUPPORTED);
+    return;
+  }
+  if (threadIdx.x == 0) {
+    const double r = ratio_of(m, ex, *s_ws_m, *s_ws_e);
+    const double a = sqrt(r * r);
+    const double p = a * a * (double)cnt / (double)s_nn;
+    int mti = *s_mti;
+    const double u = draw_uniform_real(mt, mti);
+    *s_mti = mti;
+    s_acc = u < p;
+    if (!isfinite(p)) atomicOr(eng.status, ST_NONFINITE);
+    s_m = m;
+    s_e = ex;
+    s_skip = (na == sa && nb == sb);
+  }
+  __syncthreads();
+  if (s_acc) {
+    if (threadIdx.x == 0) {
+      *s_ws_m = s_m;
+      *s_ws_e = s_e;
+    }
+    if (!s_skip) {
+      if (threadIdx.x == 0) {
+        eng.conf[l1a * md.L2 + l2a] = (short)na;
+        eng.conf[l1b * md.L2 + l2b] = (short)nb;
+        *s_h0_valid = 0;
+        *accepted += 1;
+        // E[c] stays valid, E[c+1..] do not; F[c+2..] stays valid
+        if (*eng.strip_eupto > c) *eng.strip_eupto = c;
+      }
+      eng.invalidate_site(l1a, l2a);
+      eng.invalidate_site(l1b, l2b);
+    }
+  }
+  __syncthreads();
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Slots sl, T* scratch, const T* ones,
+                                                         int nsweeps, int observe, int rec_base) {
+  __shared__ short s_conf[kMaxSites];
+  __shared__ unsigned char s_valid[4 * kMaxL];
+  __shared__ int s_eE[kMaxL + 1], s_eF[kMaxL + 1];
+  __shared__ T s_red[kWarps];
+  __shared__ double s_dred[kWarps];
+  __shared__ int s_mti, s_ws_e, s_h0_valid, s_h0_e;
+  __shared__ double s_ws_m, s_h0_m;
+  __shared__ int s_strip_kind, s_strip_idx, s_strip_eupto, s_strip_ffrom;
+  __shared__ int64_t s_accepted;
+  __shared__ double s_fl[4];
+  if (threadIdx.x < 4) s_fl[threadIdx.x] = 0.0;
+  __syncthreads();
+  const int nsite = md.L1 * md.L2;
+  Engine<T> eng{{md, sl, scratch + (long long)blockIdx.x * sl.stride, (const T*)md.A,
+                 sl.ldims + (long long)blockIdx.x * 4 * kMaxL * kMaxL * 3, sl.lexp + (long long)blockIdx.x * 4 * kMaxL,
+                 sl.order + (long long)blockIdx.x * md.cut * md.Dmax, s_conf, s_valid, s_eE, s_eF, s_red, s_dred, s_fl},
+                ones, ch.status, &s_strip_kind, &s_strip_idx, &s_strip_eupto, &s_strip_ffrom};
+  double* delta = sl.delta + (long long)blockIdx.x * md.n_params;
+  double* edelta = sl.edelta + (long long)blockIdx.x * md.n_params;
+  double* contrib = sl.contrib + (long long)blockIdx.x * md.n_terms;
+  for (int b = blockIdx.x; b < ch.B; b += gridDim.x) {
+    for (int i = threadIdx.x; i < nsite; i += blockDim.x) s_conf[i] = (short)ch.conf[(long long)b * nsite + i];
+    for (int i = threadIdx.x; i < 4 * kMaxL; i += blockDim.x) s_valid[i] = 0;
+    if (threadIdx.x == 0) {
+      s_mti = ch.mti[b];
+      s_h0_valid = 0;
+      s_strip_kind = -1;
+      s_accepted = 0;
+    }
+    __syncthreads();
+    uint64_t* mt = ch.mt + (long long)b * kMtN;
+    for (int sw = 0; sw < nsweeps; ++sw) {
+      // ws = hole(())  (sampling.py:146-148)
+      {
+        double m;
+        int e;
+        eng.hole0(m, e);
+        if (threadIdx.x == 0) {
+          s_ws_m = m;
+          s_ws_e = e;
+          s_h0_m = m;
+          s_h0_e = e;
+          s_h0_valid = 1;
+        }
+        __syncthreads();
+      }
+      // horizontal bonds, row-major (sampling.py:159-177)
+      for (int l1 = 0; l1 < md.L1; ++l1) {
+        bool any = false;
+        for (int l2 = 0; l2 + 1 < md.L2; ++l2) any |= md.hterm[l1 * md.L2 + l2] >= 0;
+        if (!any) continue;
+        eng.strip_begin(0, l1);
+        for (int l2 = 0; l2 + 1 < md.L2; ++l2) {
+          const int t = md.hterm[l1 * md.L2 + l2];
+          if (t < 0) continue;
+          single_term(eng, md, 0, l1, l2, t, mt, &s_mti, &s_ws_m, &s_ws_e, &s_h0_valid, &s_h0_m, &s_h0_e, &s_accepted);
+        }
+      }
+      // vertical bonds, column-major (sampling.py:178-186)
+      for (int l2 = 0; l2 < md.L2; ++l2) {
+        bool any = false;
+        for (int l1 = 0; l1 + 1 < md.L1; ++l1) any |= md.vterm[l1 * md.L2 + l2] >= 0;
+        if (!any) continue;
+        eng.strip_begin(1, l2);
+        for (int l1 = 0; l1 + 1 < md.L1; ++l1) {
+          const int t = md.vterm[l1 * md.L2 + l2];
+          if (t < 0) continue;
+          single_term(eng, md, 1, l2, l1, t, mt, &s_mti, &s_ws_m, &s_ws_e, &s_h0_valid, &s_h0_m, &s_h0_e, &s_accepted);
+        }
+      }
+      if (!observe) continue;
+      // ---------------- Observer.__call__ (observer.py:313-415) ----------------
+      double ws_m;
+      int ws_e;
+      eng.hole0(ws_m, ws_e);
+      __shared__ double s_rw, s_ws;
+      if (threadIdx.x == 0) {
+        const double r = ratio_of(ws_m, ws_e, s_ws_m, s_ws_e);  // ws / ws_sweep
+        s_rw = r * r;                                          // |ws|^2 / possibility
+        if (ws_m == 0.0) atomicOr(ch.status, ST_ZERO_WS);
+      }
+      for (int t = threadIdx.x; t < md.n_terms; t += blockDim.x) contrib[t] = 0.0;
+      __syncthreads();
+      const double rw = s_rw;
+      const bool zero_ws = (ws_m == 0.0);
+      // energy terms, grouped by strip; contributions kept per term and summed in term order
+      for (int kind = 0; kind < 2 && !zero_ws; ++kind) {
+        const int nl = kind == 0 ? md.L1 : md.L2;
+        const int len = kind == 0 ? md.L2 : md.L1;
+        for (int idx = 0; idx < nl; ++idx) {
+          eng.strip_begin(kind, idx);
+          eng.strip_advance(kind, idx, len);
+          for (int c = 0; c + 1 < len; ++c) {
+            int l1a, l2a, l1b, l2b;
+            eng.strip_site_rc(kind, idx, c, l1a, l2a);
+            eng.strip_site_rc(kind, idx, c + 1, l1b, l2b);
+            const int t = kind == 0 ? md.hterm[l1a * md.L2 + l2a] : md.vterm[l1a * md.L2 + l2a];
+            if (t < 0) continue;
+            const int flip = md.hflip[t];
+            const int sa = s_conf[l1a * md.L2 + l2a], sb = s_conf[l1b * md.L2 + l2b];
+            const int key = (flip ? sb : sa) * md.P + (flip ? sa : sb);
+            const int cnt = md.tab_cnt[t * md.P * md.P + key];
+            double total = 0.0;
+            for (int k = 0; k < cnt; ++k) {
+              const int out = md.tab_out[md.tab_off[t * md.P * md.P + key] + k];
+              const double v = md.tab_val[md.tab_off[t * md.P * md.P + key] + k];
+              const int o0 = out / md.P, o1 = out % md.P;
+              const int na = flip ? o1 : o0, nb = flip ? o0 : o1;
+              if (na == sa && nb == sb) {
+                total += v;
+              } else if (na != sa && nb != sb) {
+                double m;
+                int e;
+                eng.strip_replace2(kind, idx, c, na, nb, m, e);
+                if (m != 0.0) total += v * ratio_of(m, e, ws_m, ws_e);
+              } else {
+                if (threadIdx.x == 0) atomicOr(ch.status, ST_UNSUPPORTED);
+              }
+            }
+            if (threadIdx.x == 0) contrib[t] = total;
+          }
+        }
+      }
+      __syncthreads();
+      __shared__ double s_eloc;
+      if (threadIdx.x == 0) {
+        double e = 0.0;
+        for (int t = 0; t < md.n_terms; ++t) e += contrib[t];
+        s_eloc = e;
+      }
+      __syncthreads();
+      const double eloc = s_eloc;
+      if (!zero_ws) {
+        // holes: d psi / d A[l1,l2] / ws, accumulated with weight rw and E_loc * rw
+        for (int l1 = 0; l1 < md.L1; ++l1) {
+          eng.strip_begin(0, l1);
+          eng.strip_advance(0, l1, md.L2);
+          for (int l2 = 0; l2 < md.L2; ++l2) {
+            const Dims3 ed = eng.Edims(0, l1, l2);
+            const Dims3 fd = eng.Fdims(0, l1, l2 + 1);
+            T* h = scratch + (long long)blockIdx.x * sl.stride + sl.o_h;
+            T* h1 = scratch + (long long)blockIdx.x * sl.stride + sl.o_t1;
+            T* h2 = scratch + (long long)blockIdx.x * sl.stride + sl.o_t2;
+            strip_hole(eng.Ebuf(l2), ed.a, ed.p, ed.b, eng.lsite(F_UP, l1 - 1, l2), eng.lsdim(F_UP, l1 - 1, l2),
+                       eng.lsite(F_DOWN, l1 + 1, l2), eng.lsdim(F_DOWN, l1 + 1, l2), eng.Fbuf(l2 + 1), fd.p, h1, h2, h);
+            {
+              const Dims3 ud = eng.lsdim(F_UP, l1 - 1, l2), dd = eng.lsdim(F_DOWN, l1 + 1, l2);
+              eng.count(3, 2.0 * ((double)ed.p * ed.b * ud.p * ud.b * ed.a + (double)ed.p * ud.p * ud.b * dd.p * dd.b * ed.b +
+                                  (double)ud.p * dd.p * ed.p * fd.p * ud.b * dd.b));
+            }
+            const int ex = s_eE[l2] + s_eF[l2 + 1] + eng.lexpo(F_UP, l1 - 1) + eng.lexpo(F_DOWN, l1 + 1);
+            const double f = ldexp(1.0 / ws_m, ex - ws_e) * rw;
+            const int id = l1 * md.L2 + l2;
+            const int* d = md.dims + id * 4;
+            const long long n = (long long)d[0] * d[1] * d[2] * d[3];
+            const long long base = md.off[id] + (long long)s_conf[id] * n;
+            for (long long q = threadIdx.x; q < n; q += blockDim.x) {
+              const double hv = (double)h[q] * f;
+              delta[base + q] += hv;
+              edelta[base + q] += eloc * hv;
+            }
+            __syncthreads();
+          }
+        }
+      }
+      if (threadIdx.x == 0) {
+        double* acc = ch.acc + (long long)b * 8;
+        acc[0] += 1.0;
+        if (!zero_ws) {
+          acc[1] += rw;
+          acc[2] += rw * rw;
+          acc[3] += log(fabs(ws_m)) + (double)ws_e * 0.6931471805599453;
+          acc[4] += eloc * rw;
+          acc[5] += eloc * rw * rw;
+          acc[6] += eloc * eloc * rw * rw;
+        }
+        const long long r = (long long)(rec_base + sw) * ch.B + b;
+        if (ch.rec_eloc) {
+          ch.rec_eloc[r] = eloc;
+          ch.rec_logws[r] = log(fabs(ws_m)) + (double)ws_e * 0.6931471805599453;
+          ch.rec_rw[r] = rw;
+        }
+      }
+      __syncthreads();
+    }
+    // write back the chain
+    for (int i = threadIdx.x; i < nsite; i += blockDim.x) ch.conf[(long long)b * nsite + i] = s_conf[i];
+    if (threadIdx.x == 0) {
+      ch.mti[b] = s_mti;
+      ch.ws_m[b] = s_ws_m;
+      ch.ws_e[b] = s_ws_e;
+      ch.accepted[b] += s_accepted;
+      ch.acc[(long long)b * 8 + 7] += (double)s_accepted;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 4) sl.flops[(long long)blockIdx.x * 4 + threadIdx.x] += s_fl[threadIdx.x];
+}
+
+// amplitude hole(()) of arbitrary configurations (no RNG, no accumulators)
+template <class T>
+__global__ void __launch_bounds__(kThreads) amplitude_kernel(Model md, Slots sl, T* scratch, const T* ones, int B,
+                                                             const int32_t* confs, double* out_m, int32_t* out_e,
+                                                             int32_t* status) {
+  __shared__ short s_conf[kMaxSites];
+  __shared__ unsigned char s_valid[4 * kMaxL];
+  __shared__ int s_eE[kMaxL + 1], s_eF[kMaxL + 1];
+  __shared__ T s_red[kWarps];
+  __shared__ double s_dred[kWarps];
+  __shared__ int s_strip_kind, s_strip_idx, s_strip_eupto, s_strip_ffrom;
+  __shared__ double s_fl[4];
+  if (threadIdx.x < 4) s_fl[threadIdx.x] = 0.0;
+  __syncthreads();
+  const int nsite = md.L1 * md.L2;
+  Engine<T> eng{{md, sl, scratch + (long long)blockIdx.x * sl.stride, (const T*)md.A,
+                 sl.ldims + (long long)blockIdx.x * 4 * kMaxL * kMaxL * 3, sl.lexp + (long long)blockIdx.x * 4 * kMaxL,
+                 sl.order + (long long)blockIdx.x * md.cut * md.Dmax, s_conf, s_valid, s_eE, s_eF, s_red, s_dred, s_fl},
+                ones, status, &s_strip_kind, &s_strip_idx, &s_strip_eupto, &s_strip_ffrom};
+  for (int b = blockIdx.x; b < B; b += gridDim.x) {
+    for (int i = threadIdx.x; i < nsite; i += blockDim.x) s_conf[i] = (short)confs[(long long)b * nsite + i];
+    for (int i = threadIdx.x; i < 4 * kMaxL; i += blockDim.x) s_valid[i] = 0;
+    __syncthreads();
+    double m;
+    int e;
+    eng.hole0(m, e);
+    if (threadIdx.x == 0) {
+      out_m[b] = m;
+      out_e[b] = e;
+    }
+    __syncthreads();
+  }
+}
+
+// sum the per-slot gradient accumulators in slot order (deterministic)
+__global__ void reduce_slots(const double* __restrict__ src, int nslots, long long n, double* __restrict__ dst) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int k = 0; k < nslots; ++k) s += src[(long long)k * n + i];
+    dst[i] = s;
+  }
+}
+
+template <class T> __global__ void fill_ones(T* p) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) p[0] = (T)1;
+}
+
+template __global__ void sweep_kernel<double>(Model, Chains, Slots, double*, const double*, int, int, int);
+template __global__ void sweep_kernel<float>(Model, Chains, Slots, float*, const float*, int, int, int);
+template __global__ void amplitude_kernel<double>(Model, Slots, double*, const double*, int, const int32_t*, double*,
+                                                  int32_t*, int32_t*);
+template __global__ void amplitude_kernel<float>(Model, Slots, float*, const float*, int, const int32_t*, double*,
+                                                 int32_t*, int32_t*);
+template __global__ void fill_ones<double>(double*);
+template __global__ void fill_ones<float>(float*);
+
+}  // namespace tnsp

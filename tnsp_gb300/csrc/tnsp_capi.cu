@@ -1,0 +1,684 @@
+// C ABI of the sampler (declared in include/tnsp_gb300.h).  Host-side plan, buffers and
+// launches; the kernels are in sampler.cu (compiled into this translation unit).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/tnsp_gb300.h"
+#include "sampler.cu"
+
+using namespace tnsp;
+
+struct tnsp_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // lattice
+  bool has_lattice = false, has_model = false;
+  int L1 = 0, L2 = 0, P = 0, cut = 0, Dmax = 0;
+  std::vector<int> dims;
+  std::vector<long long> off;
+  long long n_params = 0;
+  double* dA64 = nullptr;
+  float* dA32 = nullptr;
+  int* d_dims = nullptr;
+  long long* d_off = nullptr;
+  // model
+  int n_terms = 0;
+  int* d_term_sites = nullptr;
+  int* d_hterm = nullptr;
+  int* d_vterm = nullptr;
+  int* d_hflip = nullptr;
+  int* d_tab_off = nullptr;
+  int* d_tab_cnt = nullptr;
+  int* d_tab_out = nullptr;
+  double* d_tab_val = nullptr;
+  // chains
+  int B = 0, precision = TNSP_FP64;
+  int32_t* d_conf = nullptr;
+  uint64_t* d_mt = nullptr;
+  int32_t* d_mti = nullptr;
+  double* d_ws_m = nullptr;
+  int32_t* d_ws_e = nullptr;
+  int64_t* d_accepted = nullptr;
+  double* d_acc = nullptr;
+  int32_t* d_status = nullptr;
+  double* d_rec = nullptr;  // 3 x rec_cap x B
+  int rec_cap = 0, rec_n = 0;
+  // slots
+  int nslots = 0;
+  Slots slots{};
+  size_t elem = 8;
+  void* d_scratch = nullptr;
+  void* d_ones = nullptr;
+  int* d_ldims = nullptr;
+  int* d_lexp = nullptr;
+  int* d_order = nullptr;
+  double* d_delta = nullptr;
+  double* d_edelta = nullptr;
+  double* d_contrib = nullptr;
+  double* d_red = nullptr;
+  double* d_flops = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0;
+  long long last_launches = 0;
+};
+
+namespace {
+
+int fail(tnsp_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define CK(call)                                                                                       \
+  do {                                                                                                 \
+    cudaError_t e_ = (call);                                                                           \
+    if (e_ != cudaSuccess) return fail(ctx, e_ == cudaErrorMemoryAllocation ? TNSP_E_NOMEM : TNSP_E_CUDA, \
+                                       std::string(#call) + ": " + cudaGetErrorString(e_));            \
+  } while (0)
+
+template <class T> void dfree(T*& p) {
+  if (p) cudaFree((void*)p);
+  p = nullptr;
+}
+
+void free_slots(tnsp_ctx* c) {
+  dfree(c->d_scratch);
+  dfree(c->d_ones);
+  dfree(c->d_ldims);
+  dfree(c->d_lexp);
+  dfree(c->d_order);
+  dfree(c->d_delta);
+  dfree(c->d_edelta);
+  dfree(c->d_contrib);
+  dfree(c->d_red);
+  dfree(c->d_flops);
+  c->nslots = 0;
+}
+
+void free_chains(tnsp_ctx* c) {
+  dfree(c->d_conf);
+  dfree(c->d_mt);
+  dfree(c->d_mti);
+  dfree(c->d_ws_m);
+  dfree(c->d_ws_e);
+  dfree(c->d_accepted);
+  dfree(c->d_acc);
+  dfree(c->d_rec);
+  c->rec_cap = 0;
+  c->rec_n = 0;
+  c->B = 0;
+}
+
+void free_model(tnsp_ctx* c) {
+  dfree(c->d_term_sites);
+  dfree(c->d_hterm);
+  dfree(c->d_vterm);
+  dfree(c->d_hflip);
+  dfree(c->d_tab_off);
+  dfree(c->d_tab_cnt);
+  dfree(c->d_tab_out);
+  dfree(c->d_tab_val);
+  c->has_model = false;
+}
+
+void free_lattice(tnsp_ctx* c) {
+  dfree(c->dA64);
+  dfree(c->dA32);
+  dfree(c->d_dims);
+  dfree(c->d_off);
+  c->has_lattice = false;
+}
+
+Model make_model(tnsp_ctx* c) {
+  Model m{};
+  m.L1 = c->L1;
+  m.L2 = c->L2;
+  m.P = c->P;
+  m.cut = c->cut;
+  m.Dmax = c->Dmax;
+  m.dims = c->d_dims;
+  m.off = c->d_off;
+  m.A = c->precision == TNSP_FP64 ? (const void*)c->dA64 : (const void*)c->dA32;
+  m.n_terms = c->n_terms;
+  m.term_sites = c->d_term_sites;
+  m.hterm = c->d_hterm;
+  m.vterm = c->d_vterm;
+  m.hflip = c->d_hflip;
+  m.tab_off = c->d_tab_off;
+  m.tab_cnt = c->d_tab_cnt;
+  m.tab_out = c->d_tab_out;
+  m.tab_val = c->d_tab_val;
+  m.n_params = c->n_params;
+  return m;
+}
+
+Chains make_chains(tnsp_ctx* c) {
+  Chains ch{};
+  ch.B = c->B;
+  ch.conf = c->d_conf;
+  ch.mt = c->d_mt;
+  ch.mti = c->d_mti;
+  ch.ws_m = c->d_ws_m;
+  ch.ws_e = c->d_ws_e;
+  ch.accepted = c->d_accepted;
+  ch.acc = c->d_acc;
+  ch.status = c->d_status;
+  if (c->d_rec) {
+    ch.rec_eloc = c->d_rec;
+    ch.rec_logws = c->d_rec + (size_t)c->rec_cap * c->B;
+    ch.rec_rw = c->d_rec + 2 * (size_t)c->rec_cap * c->B;
+  }
+  return ch;
+}
+
+// scratch layout of one slot (elements of the sampler's element type)
+void plan_slots(tnsp_ctx* c, Slots& s) {
+  const long long cut = c->cut, D = c->Dmax, Lmax = std::max(c->L1, c->L2);
+  const long long chi = cut * D;
+  s.capB = cut * D * cut;
+  s.capT = chi * D * chi;
+  s.capR = chi * chi;
+  s.capE = cut * D * cut;
+  s.capS = D * D * D * cut * cut;
+  s.capH = D * D * D * D;
+  long long o = 0;
+  auto take = [&](long long n) {
+    const long long r = o;
+    o += (n + 31) / 32 * 32;
+    return r;
+  };
+  s.o_lines[F_UP] = take((long long)c->L1 * c->L2 * s.capB);
+  s.o_lines[F_DOWN] = take((long long)c->L1 * c->L2 * s.capB);
+  s.o_lines[F_LEFT] = take((long long)c->L2 * c->L1 * s.capB);
+  s.o_lines[F_RIGHT] = take((long long)c->L2 * c->L1 * s.capB);
+  s.o_T = take((Lmax + 2) * s.capT);
+  s.o_R = take(s.capR);
+  s.o_tau = take(chi);
+  s.o_X = take(chi * chi);
+  s.o_V = take(chi * chi);
+  s.o_sig = take(chi);
+  s.o_E = take((Lmax + 1) * s.capE);
+  s.o_F = take((Lmax + 1) * s.capE);
+  s.o_t1 = take(s.capS);
+  s.o_t2 = take(s.capS);
+  s.o_w0 = take(s.capE);
+  s.o_w1 = take(s.capE);
+  s.o_h = take(s.capH);
+  s.stride = o;
+}
+
+int ensure_slots(tnsp_ctx* ctx) {
+  if (ctx->nslots > 0) return 0;
+  int sms = 0;
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  Slots s{};
+  plan_slots(ctx, s);
+  ctx->elem = ctx->precision == TNSP_FP64 ? 8 : 4;
+  // as many resident blocks as fit: 2 per SM, bounded by a scratch budget of 24 GB
+  long long want = 2LL * sms;
+  const long long per = s.stride * (long long)ctx->elem + 2LL * ctx->n_params * 8;
+  const long long budget = 24LL << 30;
+  want = std::min(want, std::max(1LL, budget / std::max(1LL, per)));
+  want = std::min<long long>(want, std::max(1, ctx->B));
+  ctx->nslots = (int)want;
+  CK(cudaMalloc(&ctx->d_scratch, (size_t)s.stride * ctx->elem * ctx->nslots));
+  CK(cudaMalloc(&ctx->d_ones, 16));
+  CK(cudaMalloc((void**)&ctx->d_ldims, sizeof(int) * 4 * kMaxL * kMaxL * 3 * ctx->nslots));
+  CK(cudaMalloc((void**)&ctx->d_lexp, sizeof(int) * 4 * kMaxL * ctx->nslots));
+  CK(cudaMalloc((void**)&ctx->d_order, sizeof(int) * ctx->cut * ctx->Dmax * ctx->nslots));
+  CK(cudaMalloc((void**)&ctx->d_delta, sizeof(double) * ctx->n_params * ctx->nslots));
+  CK(cudaMalloc((void**)&ctx->d_edelta, sizeof(double) * ctx->n_params * ctx->nslots));
+  CK(cudaMalloc((void**)&ctx->d_contrib, sizeof(double) * std::max(1, ctx->n_terms) * ctx->nslots));
+  CK(cudaMalloc((void**)&ctx->d_red, sizeof(double) * ctx->n_params * 2));
+  CK(cudaMalloc((void**)&ctx->d_flops, sizeof(double) * 4 * ctx->nslots));
+  CK(cudaMemsetAsync(ctx->d_flops, 0, sizeof(double) * 4 * ctx->nslots, ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_delta, 0, sizeof(double) * ctx->n_params * ctx->nslots, ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_edelta, 0, sizeof(double) * ctx->n_params * ctx->nslots, ctx->stream));
+  if (ctx->precision == TNSP_FP64)
+    fill_ones<double><<<1, 32, 0, ctx->stream>>>((double*)ctx->d_ones);
+  else
+    fill_ones<float><<<1, 32, 0, ctx->stream>>>((float*)ctx->d_ones);
+  CK(cudaGetLastError());
+  s.ldims = ctx->d_ldims;
+  s.lexp = ctx->d_lexp;
+  s.order = ctx->d_order;
+  s.delta = ctx->d_delta;
+  s.edelta = ctx->d_edelta;
+  s.contrib = ctx->d_contrib;
+  s.flops = ctx->d_flops;
+  ctx->slots = s;
+  return 0;
+}
+
+void seed_mt(uint64_t seed, uint64_t* mt) {
+  mt[0] = seed;
+  for (int i = 1; i < kMtN; ++i) mt[i] = 6364136223846793005ull * (mt[i - 1] ^ (mt[i - 1] >> 62)) + (uint64_t)i;
+}
+
+uint64_t host_mt_next(uint64_t* mt, int& mti) {
+  if (mti >= kMtN) {
+    for (int i = 0; i < kMtN; ++i) {
+      const uint64_t x = (mt[i] & 0xFFFFFFFF80000000ull) | (mt[(i + 1) % kMtN] & 0x7FFFFFFFull);
+      uint64_t xa = x >> 1;
+      if (x & 1ull) xa ^= 0xB5026F5AA96619E9ull;
+      mt[i] = mt[(i + 156) % kMtN] ^ xa;
+    }
+    mti = 0;
+  }
+  return mt[mti++];  // tempering not needed for discarded draws
+}
+
+}  // namespace
+
+extern "C" {
+
+int tnsp_ctx_create(tnsp_ctx** out, int device, void* stream) {
+  if (!out) return TNSP_E_ARG;
+  tnsp_ctx* ctx = new tnsp_ctx();
+  ctx->device = device;
+  ctx->stream = (cudaStream_t)stream;
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) {
+    delete ctx;
+    *out = nullptr;
+    return TNSP_E_CUDA;
+  }
+  if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) {
+    delete ctx;
+    *out = nullptr;
+    return TNSP_E_CUDA;
+  }
+  if (cudaMalloc((void**)&ctx->d_status, sizeof(int32_t)) != cudaSuccess ||
+      cudaMemset(ctx->d_status, 0, sizeof(int32_t)) != cudaSuccess) {
+    delete ctx;
+    *out = nullptr;
+    return TNSP_E_CUDA;
+  }
+  *out = ctx;
+  return TNSP_OK;
+}
+
+int tnsp_ctx_destroy(tnsp_ctx* ctx) {
+  if (!ctx) return TNSP_E_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  free_slots(ctx);
+  free_chains(ctx);
+  free_model(ctx);
+  free_lattice(ctx);
+  dfree(ctx->d_status);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  delete ctx;
+  return TNSP_OK;
+}
+
+const char* tnsp_last_error(tnsp_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int tnsp_lattice_upload(tnsp_ctx* ctx, int L1, int L2, int P, const int* dims, const double* tensors, int cut) {
+  if (!ctx) return TNSP_E_ARG;
+  if (L1 < 1 || L2 < 1 || L1 > kMaxL || L2 > kMaxL) return fail(ctx, TNSP_E_ARG, "lattice extent out of range (1..16)");
+  if (P < 1 || P > 64) return fail(ctx, TNSP_E_ARG, "physical dimension out of range");
+  if (cut < 1) return fail(ctx, TNSP_E_ARG, "cut dimension must be positive");
+  if (!dims || !tensors) return fail(ctx, TNSP_E_ARG, "null dims or tensors");
+  CK(cudaSetDevice(ctx->device));
+  std::vector<int> dv(dims, dims + (size_t)L1 * L2 * 4);
+  int Dmax = 1;
+  std::vector<long long> off(L1 * L2);
+  long long total = 0;
+  for (int l1 = 0; l1 < L1; ++l1)
+    for (int l2 = 0; l2 < L2; ++l2) {
+      const int id = l1 * L2 + l2;
+      const int* d = &dv[id * 4];
+      for (int k = 0; k < 4; ++k) {
+        if (d[k] < 1) return fail(ctx, TNSP_E_ARG, "bond extents must be >= 1");
+        Dmax = std::max(Dmax, d[k]);
+      }
+      if ((l1 == 0 && d[0] != 1) || (l1 == L1 - 1 && d[1] != 1) || (l2 == 0 && d[2] != 1) ||
+          (l2 == L2 - 1 && d[3] != 1))
+        return fail(ctx, TNSP_E_ARG, "bonds leaving the open lattice must have extent 1");
+      if (l2 + 1 < L2 && d[3] != dv[(id + 1) * 4 + 2]) return fail(ctx, TNSP_E_ARG, "R/L bond extents differ");
+      if (l1 + 1 < L1 && d[1] != dv[(id + L2) * 4 + 0]) return fail(ctx, TNSP_E_ARG, "D/U bond extents differ");
+      off[id] = total;
+      total += (long long)P * d[0] * d[1] * d[2] * d[3];
+    }
+  for (long long i = 0; i < total; ++i)
+    if (!std::isfinite(tensors[i])) return fail(ctx, TNSP_E_ARG, "non-finite element in the site tensors");
+  const bool reshape = ctx->has_lattice && (L1 != ctx->L1 || L2 != ctx->L2 || P != ctx->P || cut != ctx->cut ||
+                                            Dmax != ctx->Dmax || dv != ctx->dims);
+  if (reshape) {
+    free_slots(ctx);
+    free_chains(ctx);
+    free_model(ctx);
+  }
+  if (!ctx->has_lattice || reshape) {
+    free_lattice(ctx);
+    CK(cudaMalloc((void**)&ctx->dA64, sizeof(double) * total));
+    CK(cudaMalloc((void**)&ctx->dA32, sizeof(float) * total));
+    CK(cudaMalloc((void**)&ctx->d_dims, sizeof(int) * dv.size()));
+    CK(cudaMalloc((void**)&ctx->d_off, sizeof(long long) * off.size()));
+  }
+  std::vector<float> a32(tensors, tensors + total);
+  CK(cudaMemcpyAsync(ctx->dA64, tensors, sizeof(double) * total, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->dA32, a32.data(), sizeof(float) * total, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_dims, dv.data(), sizeof(int) * dv.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_off, off.data(), sizeof(long long) * off.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->L1 = L1;
+  ctx->L2 = L2;
+  ctx->P = P;
+  ctx->cut = cut;
+  ctx->Dmax = Dmax;
+  ctx->dims = dv;
+  ctx->off = off;
+  ctx->n_params = total;
+  ctx->has_lattice = true;
+  return TNSP_OK;
+}
+
+int tnsp_model_upload(tnsp_ctx* ctx, int n_terms, const int* sites, const int* offsets, const int* counts,
+                      int n_entries, const int* out_index, const double* values) {
+  if (!ctx) return TNSP_E_ARG;
+  if (!ctx->has_lattice) return fail(ctx, TNSP_E_STATE, "upload the lattice first");
+  if (n_terms < 0 || n_entries < 0) return fail(ctx, TNSP_E_ARG, "negative sizes");
+  CK(cudaSetDevice(ctx->device));
+  const int L1 = ctx->L1, L2 = ctx->L2, P = ctx->P;
+  std::vector<int> hterm(L1 * L2, -1), vterm(L1 * L2, -1), hflip(std::max(1, n_terms), 0);
+  for (int t = 0; t < n_terms; ++t) {
+    const int a1 = sites[t * 4], a2 = sites[t * 4 + 1], b1 = sites[t * 4 + 2], b2 = sites[t * 4 + 3];
+    if (a1 < 0 || a1 >= L1 || b1 < 0 || b1 >= L1 || a2 < 0 || a2 >= L2 || b2 < 0 || b2 >= L2)
+      return fail(ctx, TNSP_E_ARG, "term site out of range");
+    int f1 = a1, f2 = a2, flip = 0;
+    if (b1 < a1 || (b1 == a1 && b2 < a2)) {
+      f1 = b1;
+      f2 = b2;
+      flip = 1;
+    }
+    const int g1 = flip ? a1 : b1, g2 = flip ? a2 : b2;
+    int* slot = nullptr;
+    if (g1 == f1 && g2 == f2 + 1)
+      slot = &hterm[f1 * L2 + f2];
+    else if (g2 == f2 && g1 == f1 + 1)
+      slot = &vterm[f1 * L2 + f2];
+    else
+      return fail(ctx, TNSP_E_ARG, "only nearest-neighbour two-site terms are supported");
+    if (*slot >= 0) return fail(ctx, TNSP_E_ARG, "several terms on one bond");
+    *slot = t;
+    hflip[t] = flip;
+    for (int i = 0; i < P * P; ++i) {
+      const int cnt = counts[t * P * P + i];
+      if (cnt > 0 && (offsets[t * P * P + i] < 0 || offsets[t * P * P + i] + cnt > n_entries))
+        return fail(ctx, TNSP_E_ARG, "table entry range out of bounds");
+    }
+  }
+  for (int e = 0; e < n_entries; ++e)
+    if (out_index[e] < 0 || out_index[e] >= P * P) return fail(ctx, TNSP_E_ARG, "table output index out of range");
+  free_model(ctx);
+  const size_t tp = (size_t)std::max(1, n_terms) * P * P;
+  CK(cudaMalloc((void**)&ctx->d_term_sites, sizeof(int) * std::max(1, n_terms) * 4));
+  CK(cudaMalloc((void**)&ctx->d_hterm, sizeof(int) * L1 * L2));
+  CK(cudaMalloc((void**)&ctx->d_vterm, sizeof(int) * L1 * L2));
+  CK(cudaMalloc((void**)&ctx->d_hflip, sizeof(int) * hflip.size()));
+  CK(cudaMalloc((void**)&ctx->d_tab_off, sizeof(int) * tp));
+  CK(cudaMalloc((void**)&ctx->d_tab_cnt, sizeof(int) * tp));
+  CK(cudaMalloc((void**)&ctx->d_tab_out, sizeof(int) * std::max(1, n_entries)));
+  CK(cudaMalloc((void**)&ctx->d_tab_val, sizeof(double) * std::max(1, n_entries)));
+  if (n_terms > 0) {
+    CK(cudaMemcpy(ctx->d_term_sites, sites, sizeof(int) * n_terms * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_tab_off, offsets, sizeof(int) * n_terms * P * P, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_tab_cnt, counts, sizeof(int) * n_terms * P * P, cudaMemcpyHostToDevice));
+  }
+  if (n_entries > 0) {
+    CK(cudaMemcpy(ctx->d_tab_out, out_index, sizeof(int) * n_entries, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_tab_val, values, sizeof(double) * n_entries, cudaMemcpyHostToDevice));
+  }
+  CK(cudaMemcpy(ctx->d_hterm, hterm.data(), sizeof(int) * L1 * L2, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_vterm, vterm.data(), sizeof(int) * L1 * L2, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_hflip, hflip.data(), sizeof(int) * hflip.size(), cudaMemcpyHostToDevice));
+  ctx->n_terms = n_terms;
+  ctx->has_model = true;
+  free_slots(ctx);  // the contribution buffer depends on n_terms
+  return TNSP_OK;
+}
+
+int tnsp_chains_init(tnsp_ctx* ctx, int B, const int32_t* configs, const uint64_t* seeds, int discard,
+                     int precision) {
+  if (!ctx) return TNSP_E_ARG;
+  if (!ctx->has_lattice || !ctx->has_model) return fail(ctx, TNSP_E_STATE, "upload the lattice and the model first");
+  if (B < 1) return fail(ctx, TNSP_E_ARG, "need at least one chain");
+  if (precision != TNSP_FP64 && precision != TNSP_FP32) return fail(ctx, TNSP_E_ARG, "unknown precision");
+  if (!configs || !seeds) return fail(ctx, TNSP_E_ARG, "null configs or seeds");
+  const int ns = ctx->L1 * ctx->L2;
+  for (long long i = 0; i < (long long)B * ns; ++i)
+    if (configs[i] < 0 || configs[i] >= ctx->P) return fail(ctx, TNSP_E_ARG, "configuration index out of range");
+  CK(cudaSetDevice(ctx->device));
+  if (B != ctx->B || precision != ctx->precision) {
+    free_chains(ctx);
+    free_slots(ctx);
+    ctx->precision = precision;
+    CK(cudaMalloc((void**)&ctx->d_conf, sizeof(int32_t) * B * ns));
+    CK(cudaMalloc((void**)&ctx->d_mt, sizeof(uint64_t) * B * kMtN));
+    CK(cudaMalloc((void**)&ctx->d_mti, sizeof(int32_t) * B));
+    CK(cudaMalloc((void**)&ctx->d_ws_m, sizeof(double) * B));
+    CK(cudaMalloc((void**)&ctx->d_ws_e, sizeof(int32_t) * B));
+    CK(cudaMalloc((void**)&ctx->d_accepted, sizeof(int64_t) * B));
+    CK(cudaMalloc((void**)&ctx->d_acc, sizeof(double) * B * 8));
+    ctx->B = B;
+  }
+  std::vector<uint64_t> mt((size_t)B * kMtN);
+  std::vector<int32_t> mti(B);
+  for (int b = 0; b < B; ++b) {
+    seed_mt(seeds[b], &mt[(size_t)b * kMtN]);
+    int k = kMtN;
+    for (int d = 0; d < discard; ++d) host_mt_next(&mt[(size_t)b * kMtN], k);
+    mti[b] = k;
+  }
+  CK(cudaMemcpy(ctx->d_conf, configs, sizeof(int32_t) * B * ns, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_mt, mt.data(), sizeof(uint64_t) * mt.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_mti, mti.data(), sizeof(int32_t) * B, cudaMemcpyHostToDevice));
+  CK(cudaMemset(ctx->d_accepted, 0, sizeof(int64_t) * B));
+  CK(cudaMemset(ctx->d_acc, 0, sizeof(double) * B * 8));
+  CK(cudaMemset(ctx->d_ws_m, 0, sizeof(double) * B));
+  CK(cudaMemset(ctx->d_ws_e, 0, sizeof(int32_t) * B));
+  return ensure_slots(ctx);
+}
+
+int tnsp_observer_reset(tnsp_ctx* ctx) {
+  if (!ctx) return TNSP_E_ARG;
+  if (!ctx->B) return fail(ctx, TNSP_E_STATE, "no chains");
+  CK(cudaSetDevice(ctx->device));
+  int r = ensure_slots(ctx);
+  if (r) return r;
+  CK(cudaMemsetAsync(ctx->d_acc, 0, sizeof(double) * ctx->B * 8, ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_delta, 0, sizeof(double) * ctx->n_params * ctx->nslots, ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_edelta, 0, sizeof(double) * ctx->n_params * ctx->nslots, ctx->stream));
+  ctx->rec_n = 0;
+  return TNSP_OK;
+}
+
+int tnsp_sweep(tnsp_ctx* ctx, int nsweeps, int observe) {
+  if (!ctx) return TNSP_E_ARG;
+  if (!ctx->B) return fail(ctx, TNSP_E_STATE, "no chains");
+  if (nsweeps < 0) return fail(ctx, TNSP_E_ARG, "negative sweep count");
+  CK(cudaSetDevice(ctx->device));
+  int r = ensure_slots(ctx);
+  if (r) return r;
+  if (observe) {
+    // the per-sample record holds the samples of this call
+    if (ctx->rec_cap < nsweeps) {
+      dfree(ctx->d_rec);
+      CK(cudaMalloc((void**)&ctx->d_rec, sizeof(double) * 3 * (size_t)std::max(1, nsweeps) * ctx->B));
+      ctx->rec_cap = std::max(1, nsweeps);
+    }
+    ctx->rec_n = nsweeps;
+  }
+  Model md = make_model(ctx);
+  Chains ch = make_chains(ctx);
+  if (!observe) {
+    ch.rec_eloc = ch.rec_logws = ch.rec_rw = nullptr;
+  }
+  const int grid = ctx->nslots;
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  if (nsweeps > 0) {
+    if (ctx->precision == TNSP_FP64)
+      sweep_kernel<double><<<grid, kThreads, 0, ctx->stream>>>(md, ch, ctx->slots, (double*)ctx->d_scratch,
+                                                               (const double*)ctx->d_ones, nsweeps, observe, 0);
+    else
+      sweep_kernel<float><<<grid, kThreads, 0, ctx->stream>>>(md, ch, ctx->slots, (float*)ctx->d_scratch,
+                                                              (const float*)ctx->d_ones, nsweeps, observe, 0);
+    CK(cudaGetLastError());
+  }
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  CK(cudaEventSynchronize(ctx->ev1));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  ctx->last_ms = ms;
+  ctx->last_launches = nsweeps > 0 ? 1 : 0;
+  int32_t st = 0;
+  CK(cudaMemcpy(&st, ctx->d_status, sizeof(int32_t), cudaMemcpyDeviceToHost));
+  if (st & (TNSP_ST_SVD_NOCONV | TNSP_ST_NONFINITE | TNSP_ST_UNSUPPORTED)) {
+    char buf[128];
+    snprintf(buf, sizeof buf, "device status 0x%x (see TNSP_ST_* bits)", st);
+    return fail(ctx, TNSP_E_DEVICE, buf);
+  }
+  return TNSP_OK;
+}
+
+int tnsp_observer_read(tnsp_ctx* ctx, double* scalars, double* delta, double* edelta) {
+  if (!ctx) return TNSP_E_ARG;
+  if (!ctx->B || !ctx->nslots) return fail(ctx, TNSP_E_STATE, "no chains");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  std::vector<double> acc((size_t)ctx->B * 8);
+  CK(cudaMemcpy(acc.data(), ctx->d_acc, sizeof(double) * acc.size(), cudaMemcpyDeviceToHost));
+  if (scalars) {
+    for (int k = 0; k < 8; ++k) {
+      double s = 0;
+      for (int b = 0; b < ctx->B; ++b) s += acc[(size_t)b * 8 + k];
+      scalars[k] = s;
+    }
+  }
+  const long long n = ctx->n_params;
+  const int threads = 256;
+  const int blocks = (int)std::min<long long>((n + threads - 1) / threads, 4096);
+  if (delta) {
+    reduce_slots<<<blocks, threads, 0, ctx->stream>>>(ctx->d_delta, ctx->nslots, n, ctx->d_red);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(delta, ctx->d_red, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  if (edelta) {
+    reduce_slots<<<blocks, threads, 0, ctx->stream>>>(ctx->d_edelta, ctx->nslots, n, ctx->d_red + n);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(edelta, ctx->d_red + n, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return TNSP_OK;
+}
+
+int tnsp_samples_read(tnsp_ctx* ctx, double* eloc, double* log_ws, double* reweight) {
+  if (!ctx) return TNSP_E_ARG;
+  if (!ctx->d_rec) return fail(ctx, TNSP_E_STATE, "no observed sweeps recorded");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const size_t n = (size_t)ctx->rec_n * ctx->B;
+  const size_t cap = (size_t)ctx->rec_cap * ctx->B;
+  if (eloc) CK(cudaMemcpy(eloc, ctx->d_rec, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (log_ws) CK(cudaMemcpy(log_ws, ctx->d_rec + cap, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (reweight) CK(cudaMemcpy(reweight, ctx->d_rec + 2 * cap, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  return TNSP_OK;
+}
+
+int tnsp_chains_read(tnsp_ctx* ctx, int32_t* configs, double* log_possibility) {
+  if (!ctx) return TNSP_E_ARG;
+  if (!ctx->B) return fail(ctx, TNSP_E_STATE, "no chains");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (configs)
+    CK(cudaMemcpy(configs, ctx->d_conf, sizeof(int32_t) * ctx->B * ctx->L1 * ctx->L2, cudaMemcpyDeviceToHost));
+  if (log_possibility) {
+    std::vector<double> m(ctx->B);
+    std::vector<int32_t> e(ctx->B);
+    CK(cudaMemcpy(m.data(), ctx->d_ws_m, sizeof(double) * ctx->B, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(e.data(), ctx->d_ws_e, sizeof(int32_t) * ctx->B, cudaMemcpyDeviceToHost));
+    for (int b = 0; b < ctx->B; ++b) log_possibility[b] = 2.0 * (std::log(std::fabs(m[b])) + e[b] * 0.6931471805599453);
+  }
+  return TNSP_OK;
+}
+
+int tnsp_amplitude(tnsp_ctx* ctx, int B, const int32_t* configs, double* mantissa, int32_t* exponent) {
+  if (!ctx) return TNSP_E_ARG;
+  if (!ctx->has_lattice || !ctx->has_model) return fail(ctx, TNSP_E_STATE, "upload the lattice and the model first");
+  if (B < 1 || !configs || !mantissa || !exponent) return fail(ctx, TNSP_E_ARG, "bad arguments");
+  const int ns = ctx->L1 * ctx->L2;
+  for (long long i = 0; i < (long long)B * ns; ++i)
+    if (configs[i] < 0 || configs[i] >= ctx->P) return fail(ctx, TNSP_E_ARG, "configuration index out of range");
+  CK(cudaSetDevice(ctx->device));
+  int r = ensure_slots(ctx);
+  if (r) return r;
+  int32_t* dconf = nullptr;
+  double* dm = nullptr;
+  int32_t* de = nullptr;
+  CK(cudaMalloc((void**)&dconf, sizeof(int32_t) * B * ns));
+  CK(cudaMalloc((void**)&dm, sizeof(double) * B));
+  CK(cudaMalloc((void**)&de, sizeof(int32_t) * B));
+  CK(cudaMemcpyAsync(dconf, configs, sizeof(int32_t) * B * ns, cudaMemcpyHostToDevice, ctx->stream));
+  Model md = make_model(ctx);
+  const int grid = std::min(ctx->nslots, B);
+  if (ctx->precision == TNSP_FP64)
+    amplitude_kernel<double><<<grid, kThreads, 0, ctx->stream>>>(md, ctx->slots, (double*)ctx->d_scratch,
+                                                                 (const double*)ctx->d_ones, B, dconf, dm, de,
+                                                                 ctx->d_status);
+  else
+    amplitude_kernel<float><<<grid, kThreads, 0, ctx->stream>>>(md, ctx->slots, (float*)ctx->d_scratch,
+                                                                (const float*)ctx->d_ones, B, dconf, dm, de,
+                                                                ctx->d_status);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(mantissa, dm, sizeof(double) * B, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(exponent, de, sizeof(int32_t) * B, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  cudaFree(dconf);
+  cudaFree(dm);
+  cudaFree(de);
+  return TNSP_OK;
+}
+
+int tnsp_device_status(tnsp_ctx* ctx, int32_t* status) {
+  if (!ctx || !status) return TNSP_E_ARG;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(status, ctx->d_status, sizeof(int32_t), cudaMemcpyDeviceToHost));
+  CK(cudaMemset(ctx->d_status, 0, sizeof(int32_t)));
+  return TNSP_OK;
+}
+
+int tnsp_last_timing(tnsp_ctx* ctx, double* ms, int64_t* launches) {
+  if (!ctx) return TNSP_E_ARG;
+  if (ms) *ms = ctx->last_ms;
+  if (launches) *launches = ctx->last_launches;
+  return TNSP_OK;
+}
+
+int tnsp_counters_read(tnsp_ctx* ctx, double* flops, int reset) {
+  if (!ctx || !flops) return TNSP_E_ARG;
+  if (!ctx->nslots) return fail(ctx, TNSP_E_STATE, "no chains");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  std::vector<double> f((size_t)4 * ctx->nslots);
+  CK(cudaMemcpy(f.data(), ctx->d_flops, sizeof(double) * f.size(), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < 4; ++k) {
+    double s = 0;
+    for (int i = 0; i < ctx->nslots; ++i) s += f[(size_t)i * 4 + k];
+    flops[k] = s;
+  }
+  if (reset) CK(cudaMemset(ctx->d_flops, 0, sizeof(double) * f.size()));
+  return TNSP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,156 @@
+"""Python handle on the C-ABI sampler (include/tnsp_gb300.h)."""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import TNSP_FP32, TNSP_FP64, ptr
+
+LN2 = 0.6931471805599453
+
+
+class TnspError(RuntimeError):
+    pass
+
+
+class Sampler:
+    """B independent sweep-sampling chains of one PEPS on one GPU.
+
+    One chain here is one reference process running ``SweepSampling`` with its own seeded
+    ``TAT.random`` engine; all chains advance together on the device.
+    """
+
+    def __init__(self, lattice, cut_dimension, device=0, stream=None):
+        self.lib = _lib.load()
+        self.ctx = ctypes.c_void_p()
+        self._check(self.lib.tnsp_ctx_create(ctypes.byref(self.ctx), device, stream), "tnsp_ctx_create")
+        self.lattice = lattice
+        self.cut = cut_dimension
+        self.B = 0
+        self.precision = TNSP_FP64
+        self._uploaded_version = None
+        self.upload()
+
+    def _check(self, code, what):
+        if code != 0:
+            msg = self.lib.tnsp_last_error(self.ctx).decode() if self.ctx else ""
+            raise TnspError(f"{what} failed ({code}): {msg}")
+
+    def close(self):
+        if self.ctx:
+            self.lib.tnsp_ctx_destroy(self.ctx)
+            self.ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---------------------------------------------------------------------------------------
+    def upload(self):
+        lat = self.lattice
+        dims = np.ascontiguousarray(lat.dims())
+        flat = np.ascontiguousarray(lat.flat_tensors())
+        self._check(
+            self.lib.tnsp_lattice_upload(self.ctx, lat.L1, lat.L2, lat.P, ptr(dims, ctypes.c_int),
+                                         ptr(flat, ctypes.c_double), self.cut), "tnsp_lattice_upload")
+        n, sites, offs, cnts, outs, vals = lat.term_arrays()
+        self._check(
+            self.lib.tnsp_model_upload(self.ctx, n, ptr(sites, ctypes.c_int), ptr(offs, ctypes.c_int),
+                                       ptr(cnts, ctypes.c_int), len(outs), ptr(outs, ctypes.c_int),
+                                       ptr(vals, ctypes.c_double)), "tnsp_model_upload")
+        self._uploaded_version = lat.version
+
+    def init_chains(self, configs, seeds, discard=0, precision=TNSP_FP64):
+        configs = np.ascontiguousarray(configs, dtype=np.int32)
+        seeds = np.ascontiguousarray(seeds, dtype=np.uint64)
+        B = seeds.shape[0]
+        if configs.ndim == 2:
+            configs = np.ascontiguousarray(np.broadcast_to(configs, (B,) + configs.shape))
+        configs = configs.reshape(B, -1)
+        self._check(
+            self.lib.tnsp_chains_init(self.ctx, B, ptr(configs, ctypes.c_int32), ptr(seeds, ctypes.c_uint64), discard,
+                                      precision), "tnsp_chains_init")
+        self.B = B
+        self.precision = precision
+
+    def sweep(self, nsweeps=1, observe=False):
+        if self._uploaded_version != self.lattice.version:
+            raise TnspError("lattice changed since upload; call upload() and init_chains() again")
+        self._check(self.lib.tnsp_sweep(self.ctx, nsweeps, 1 if observe else 0), "tnsp_sweep")
+
+    def reset_observer(self):
+        self._check(self.lib.tnsp_observer_reset(self.ctx), "tnsp_observer_reset")
+
+    def read_observer(self, with_gradient=True):
+        scalars = np.zeros(8)
+        n = sum(self.lattice[l1, l2].size for l1, l2 in self.lattice.sites())
+        delta = np.zeros(n) if with_gradient else None
+        edelta = np.zeros(n) if with_gradient else None
+        self._check(
+            self.lib.tnsp_observer_read(self.ctx, ptr(scalars, ctypes.c_double), ptr(delta, ctypes.c_double),
+                                        ptr(edelta, ctypes.c_double)), "tnsp_observer_read")
+        return scalars, delta, edelta
+
+    def read_samples(self, nsweeps):
+        eloc = np.zeros((nsweeps, self.B))
+        logws = np.zeros((nsweeps, self.B))
+        rw = np.zeros((nsweeps, self.B))
+        self._check(
+            self.lib.tnsp_samples_read(self.ctx, ptr(eloc, ctypes.c_double), ptr(logws, ctypes.c_double),
+                                       ptr(rw, ctypes.c_double)), "tnsp_samples_read")
+        return eloc, logws, rw
+
+    def read_chains(self):
+        conf = np.zeros((self.B, self.lattice.L1, self.lattice.L2), dtype=np.int32)
+        logp = np.zeros(self.B)
+        self._check(self.lib.tnsp_chains_read(self.ctx, ptr(conf, ctypes.c_int32), ptr(logp, ctypes.c_double)),
+                    "tnsp_chains_read")
+        return conf, logp
+
+    def amplitude(self, configs):
+        configs = np.ascontiguousarray(configs, dtype=np.int32)
+        B = configs.shape[0]
+        m = np.zeros(B)
+        e = np.zeros(B, dtype=np.int32)
+        self._check(
+            self.lib.tnsp_amplitude(self.ctx, B, ptr(configs.reshape(B, -1), ctypes.c_int32), ptr(m, ctypes.c_double),
+                                    ptr(e, ctypes.c_int32)), "tnsp_amplitude")
+        return m, e
+
+    def status(self):
+        st = ctypes.c_int32()
+        self._check(self.lib.tnsp_device_status(self.ctx, ctypes.byref(st)), "tnsp_device_status")
+        return st.value
+
+    def counters(self, reset=True):
+        """Algorithmic flops since the last reset: [contractions, QR, SVD, strips/holes]."""
+        f = np.zeros(4)
+        self._check(self.lib.tnsp_counters_read(self.ctx, ptr(f, ctypes.c_double), 1 if reset else 0),
+                    "tnsp_counters_read")
+        return f
+
+    def last_timing(self):
+        ms = ctypes.c_double()
+        n = ctypes.c_int64()
+        self._check(self.lib.tnsp_last_timing(self.ctx, ctypes.byref(ms), ctypes.byref(n)), "tnsp_last_timing")
+        return ms.value, n.value
+
+
+def estimators(scalars, site_number):
+    """Energy per site and error bar from the reduced accumulators (observer.py:433-469, 528-540)."""
+    count, R, RR, logws, ER, ERR, EERR, accepted = scalars
+    if ER == 0.0 or R == 0.0:
+        return 0.0, 0.0
+    expect = ER / R
+    variance = (EERR - 2 * ERR * expect + RR * expect**2) / R**2
+    dev = variance**0.5 if variance >= 0 else 0.0
+    return expect / site_number, dev / site_number
+
+
+def gradient_from(scalars, delta, edelta):
+    """``Observer.gradient`` (observer.py:542-555) for real tensors, flat layout."""
+    R = scalars[1]
+    energy = scalars[4] / R
+    return 2.0 * (edelta / R - energy * delta / R)
