@@ -23,6 +23,7 @@ extern "C" {
 #define TNSP_E_STATE (-3)      /* call out of order (no lattice, no chains, ...) */
 #define TNSP_E_DEVICE (-4)     /* a kernel reported a failure (see the status word) */
 #define TNSP_E_NOMEM (-5)      /* device allocation failed */
+#define TNSP_E_TOO_LARGE (-6)  /* problem exceeds the fixed arena of tnsp_amplitude_noalloc */
 
 /* device status word bits (tnsp_device_status) */
 #define TNSP_ST_SVD_NOCONV 1   /* one-sided Jacobi hit its sweep limit */
@@ -130,6 +131,23 @@ int tnsp_last_timing(tnsp_ctx* ctx, double* ms, int64_t* launches);
  * No reference counterpart: instrumentation for the roofline of the sampler kernel.
  */
 int tnsp_counters_read(tnsp_ctx* ctx, double* flops, int reset);
+
+/*
+ * Allocation-free variant of tnsp_amplitude, for callers that cannot call cudaMalloc (code
+ * running inside a CUDA-graph capture or a stream callback, processes whose device memory belongs
+ * to a caching allocator, hosts that forbid allocation after start-up).  No counterpart in the
+ * reference.  It needs no context: tensors (dense A[p][u][d][l][r], float64), configs
+ * (B x L1*L2 int32), mantissa (B doubles) and exponent (B int32) are caller-owned DEVICE
+ * pointers; dims (L1*L2*4 ints, as in tnsp_lattice_upload) is a host pointer; stream is a
+ * cudaStream_t or NULL.  Configuration entries must lie in [0, P): they are not checked on the device.
+ * The call is synchronous with respect to `stream`.
+ * Scratch comes from a 64 MiB array compiled into the library (held by every device that loads
+ * it); a lattice/cut whose one-chain scratch does not fit returns TNSP_E_TOO_LARGE.  The first
+ * call on a device resolves the array's address (cudaGetSymbolAddress): make it before any stream
+ * capture.  Calls share the array: calls that overlap on the GPU race and must be serialised.
+ */
+int tnsp_amplitude_noalloc(int L1, int L2, int P, const int* dims, const double* tensors, int cut, int B,
+                           const int32_t* configs, double* mantissa, int32_t* exponent, void* stream);
 
 #ifdef __cplusplus
 }

@@ -38,6 +38,10 @@ SIGNATURES = {
     "tnsp_device_status": (ctypes.c_int, [_c_void_p, _c_i32_p]),
     "tnsp_last_timing": (ctypes.c_int, [_c_void_p, _c_dbl_p, _c_i64_p]),
     "tnsp_counters_read": (ctypes.c_int, [_c_void_p, _c_dbl_p, ctypes.c_int]),
+    "tnsp_amplitude_noalloc": (ctypes.c_int, [
+        ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_int_p, _c_void_p, ctypes.c_int, ctypes.c_int, _c_void_p, _c_void_p,
+        _c_void_p, _c_void_p
+    ]),
 }
 
 _lib = None

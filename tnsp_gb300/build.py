@@ -7,7 +7,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libtnsp_gb300.so")
 SOURCES = [os.path.join(CSRC, "tnsp_capi.cu")]
-DEPS = SOURCES + [os.path.join(CSRC, f) for f in ("sampler.cu", "cta_linalg.cuh")] + [
+DEPS = SOURCES + [os.path.join(CSRC, f) for f in ("sampler.cu", "cta_linalg.cuh", "noalloc.cu")] + [
     os.path.join(os.path.dirname(HERE), "include", "tnsp_gb300.h")
 ]
 NVCC_FLAGS = [

@@ -682,3 +682,5 @@ int tnsp_counters_read(tnsp_ctx* ctx, double* flops, int reset) {
 }
 
 }  // extern "C"
+
+#include "noalloc.cu"
