@@ -59,6 +59,19 @@ const char* tnsp_last_error(tnsp_ctx* ctx);
 int tnsp_lattice_upload(tnsp_ctx* ctx, int L1, int L2, int P, const int* dims, const double* tensors, int cut);
 
 /*
+ * Declares the U(1)/Z-graded block structure of the uploaded lattice (optional; without it every
+ * charge is zero and every matrix is one block).  leg_charges[(site*4 + leg)*Dmax + i] is the charge
+ * of index i of leg U, D, L, R (Dmax = largest bond extent), phys_charges[p] the charge of physical
+ * index p, site_flux[site] the conserved sum: every nonzero A[p][u][d][l][r] must satisfy
+ * phys[p] + U[u] + D[d] + L[l] + R[r] == site_flux (checked; connected legs must carry opposite
+ * charges).  With charges, every QR and SVD of the boundary compression runs per charge sector and
+ * the truncation keeps the largest singular values over all sectors.
+ * Replaces: the Symmetry/Edge segment structure of TAT (TAT/include/TAT/structure/symmetry.hpp:94-239,
+ * edge.hpp:212-292) and its per-sector QR/SVD (TAT/include/TAT/implement/qr.hpp:310-510, svd.hpp:259-532).
+ */
+int tnsp_lattice_charges(tnsp_ctx* ctx, const int* leg_charges, const int* phys_charges, const int* site_flux);
+
+/*
  * Uploads the Hamiltonian: n_terms two-site terms in the reference's dictionary order.
  * sites[t*4 + {0,1,2,3}] = (l1, l2) of positions[0] then positions[1] of term t (nearest
  * neighbours).  For term t and input pair index i = s0*P + s1 (s0 at positions[0]) the outputs

@@ -7,10 +7,23 @@ from golden_cases import CASES, Golden
 pytestmark = pytest.mark.gpu
 
 
-def make_lattice(g):
-    from tnsp_gb300.lattice import SamplingLattice
+def make_lattice(g, charged=False):
+    """Lattice of a golden case; ``charged`` declares the reference's block structure so the device
+    factorises per charge sector."""
+    from tnsp_gb300.lattice import SamplingLattice, site_charges
     dense = g.dense_sites()
-    return SamplingLattice(g.L1, g.L2, dense[0][0].shape[0], dense, {pos: t for pos, t in g.terms()})
+    charges = None
+    if charged:
+        legs = [[None] * g.L2 for _ in range(g.L1)]
+        flux = [[0] * g.L2 for _ in range(g.L1)]
+        phys = None
+        for l1 in range(g.L1):
+            for l2 in range(g.L2):
+                meta = g.meta["sites"][f"{l1},{l2}"]
+                legs[l1][l2], phys, flux[l1][l2] = site_charges([m["name"] for m in meta],
+                                                                [[tuple(x) for x in m["segments"]] for m in meta])
+        charges = (legs, phys, flux)
+    return SamplingLattice(g.L1, g.L2, dense[0][0].shape[0], dense, {pos: t for pos, t in g.terms()}, charges)
 
 
 @pytest.fixture(scope="module")
@@ -19,10 +32,11 @@ def engine_mod():
     return engine
 
 
+@pytest.mark.parametrize("charged", [False, True])
 @pytest.mark.parametrize("name", CASES)
-def test_sweeps_and_observer_match_reference(name, engine_mod):
+def test_sweeps_and_observer_match_reference(name, charged, engine_mod):
     g = Golden(name)
-    lat = make_lattice(g)
+    lat = make_lattice(g, charged)
     z = g.z
     seeds = np.array(g.meta["chain_seeds"], dtype=np.uint64)
     B = len(seeds)
@@ -71,10 +85,11 @@ def test_amplitude_entry(name, engine_mod):
     np.testing.assert_allclose(ws, g.z["ws"][0], rtol=1e-10, atol=0)
 
 
-def test_fp32_mode_close_to_fp64(engine_mod):
+@pytest.mark.parametrize("charged", [False, True])
+def test_fp32_mode_close_to_fp64(charged, engine_mod):
     """Mixed mode: the same chains in float32 arithmetic; amplitudes and E_loc within 1e-3 relative."""
     g = Golden("heis_u1_4x4_D222_dc8")
-    lat = make_lattice(g)
+    lat = make_lattice(g, charged)
     confs = g.z["confs"][0][g.meta["n_therm"]:]
     s64 = engine_mod.Sampler(lat, g.cut)
     m64, e64 = s64.amplitude(confs)

@@ -86,3 +86,17 @@ def test_library_exports_every_declared_symbol():
     lib = _lib.load()
     for name in _lib.SIGNATURES:
         assert hasattr(lib, name), name
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_site_charges_conserve_on_reference_tensors(name):
+    """The charges derived from the reference's edges make every nonzero element conserve charge."""
+    from tnsp_gb300.lattice import site_charges
+    g = Golden(name)
+    for l1 in range(g.L1):
+        for l2 in range(g.L2):
+            meta = g.meta["sites"][f"{l1},{l2}"]
+            legs, phys, flux = site_charges([m["name"] for m in meta], [[tuple(x) for x in m["segments"]] for m in meta])
+            t = g.z[f"site_{l1}_{l2}_dense"]
+            for p, u, d, l, r in np.argwhere(t != 0):
+                assert phys[p] + legs["U"][u] + legs["D"][d] + legs["L"][l] + legs["R"][r] == flux

@@ -26,6 +26,7 @@ SIGNATURES = {
     "tnsp_last_error": (ctypes.c_char_p, [_c_void_p]),
     "tnsp_lattice_upload": (ctypes.c_int,
                             [_c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_int_p, _c_dbl_p, ctypes.c_int]),
+    "tnsp_lattice_charges": (ctypes.c_int, [_c_void_p, _c_int_p, _c_int_p, _c_int_p]),
     "tnsp_model_upload": (ctypes.c_int,
                           [_c_void_p, ctypes.c_int, _c_int_p, _c_int_p, _c_int_p, ctypes.c_int, _c_int_p, _c_dbl_p]),
     "tnsp_chains_init": (ctypes.c_int, [_c_void_p, ctypes.c_int, _c_i32_p, _c_u64_p, ctypes.c_int, ctypes.c_int]),

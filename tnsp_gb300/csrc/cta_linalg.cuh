@@ -267,4 +267,126 @@ __device__ int block_jacobi(int nv, int len, T* X, T* Vr, int max_sweeps) {
   return -1;
 }
 
+
+// ---------------------------------------------------------------------------------------------
+// block-wide integer scan and stable compaction
+// ---------------------------------------------------------------------------------------------
+// Inclusive prefix sum of one int per thread; `sh` is shared scratch of kWarps + 1 ints.  The block
+// total is returned in *total.
+__device__ __forceinline__ int block_inclusive_scan(int v, int* sh, int* total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += y;
+  }
+  __syncthreads();
+  if (lane == 31) sh[w] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int i = 0; i < kWarps; ++i) {
+      const int t = sh[i];
+      sh[i] = acc;
+      acc += t;
+    }
+    sh[kWarps] = acc;
+  }
+  __syncthreads();
+  v += sh[w];
+  *total = sh[kWarps];
+  __syncthreads();
+  return v;
+}
+
+// Writes, in increasing order, every i in [0, n) with pred(i) to out; returns the count.
+template <class Pred> __device__ int block_compact(int n, Pred pred, int* out, int* sh) {
+  const int chunk = (n + (int)blockDim.x - 1) / (int)blockDim.x;
+  const int beg = threadIdx.x * chunk;
+  const int end = beg + chunk < n ? beg + chunk : n;
+  int cnt = 0;
+  for (int i = beg; i < end; ++i) cnt += pred(i) ? 1 : 0;
+  int total;
+  int pos = block_inclusive_scan(cnt, sh, &total) - cnt;
+  for (int i = beg; i < end; ++i)
+    if (pred(i)) out[pos++] = i;
+  __syncthreads();
+  return total;
+}
+
+// ---------------------------------------------------------------------------------------------
+// column-major Householder QR (LAPACK geqr2 / org2r conventions, any orthogonal gauge is fine)
+// ---------------------------------------------------------------------------------------------
+// G: m x n column-major (ld = m), overwritten by R (upper triangle) and the reflectors below it.
+template <class T> __device__ void block_geqrf_cm(int m, int n, T* G, T* tau, T* red) {
+  const int kk = m < n ? m : n;
+  __shared__ T s_beta, s_tau, s_scale;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int j = 0; j < kk; ++j) {
+    T* gj = G + (long)j * m;
+    T part = 0;
+    for (int r = j + 1 + threadIdx.x; r < m; r += blockDim.x) part = fma(gj[r], gj[r], part);
+    const T sigma = block_sum(part, red);
+    if (threadIdx.x == 0) {
+      const T alpha = gj[j];
+      if (sigma == (T)0) {
+        s_tau = 0;
+        s_beta = alpha;
+        s_scale = 0;
+      } else {
+        T beta = sqrt(alpha * alpha + sigma);
+        if (alpha > 0) beta = -beta;
+        s_tau = (beta - alpha) / beta;
+        s_scale = (T)1 / (alpha - beta);
+        s_beta = beta;
+      }
+      tau[j] = s_tau;
+    }
+    __syncthreads();
+    const T tj = s_tau, sc = s_scale;
+    if (tj != (T)0)
+      for (int r = j + 1 + threadIdx.x; r < m; r += blockDim.x) gj[r] *= sc;
+    __syncthreads();
+    if (threadIdx.x == 0) gj[j] = s_beta;
+    if (tj != (T)0) {
+      for (int c = j + 1 + w; c < n; c += kWarps) {
+        T* gc = G + (long)c * m;
+        T d = lane == 0 ? gc[j] : (T)0;
+        for (int r = j + 1 + lane; r < m; r += 32) d = fma(gj[r], gc[r], d);
+        d = warp_sum(d) * tj;
+        if (lane == 0) gc[j] -= d;
+        for (int r = j + 1 + lane; r < m; r += 32) gc[r] -= d * gj[r];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Forms Q (m x k, first k columns of G, column-major) in place from block_geqrf_cm's reflectors.
+template <class T> __device__ void block_orgqr_cm(int m, int k, T* G, const T* tau) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int i = k - 1; i >= 0; --i) {
+    T* gi = G + (long)i * m;
+    const T ti = tau[i];
+    if (i < k - 1) {
+      if (threadIdx.x == 0) gi[i] = (T)1;
+      __syncthreads();
+      if (ti != (T)0) {
+        for (int c = i + 1 + w; c < k; c += kWarps) {
+          T* gc = G + (long)c * m;
+          T d = 0;
+          for (int r = i + lane; r < m; r += 32) d = fma(gi[r], gc[r], d);
+          d = warp_sum(d) * ti;
+          for (int r = i + lane; r < m; r += 32) gc[r] -= d * gi[r];
+        }
+      }
+      __syncthreads();
+    }
+    for (int r = i + 1 + threadIdx.x; r < m; r += blockDim.x) gi[r] *= -ti;
+    for (int r = threadIdx.x; r < i; r += blockDim.x) gi[r] = (T)0;
+    if (threadIdx.x == 0) gi[i] = (T)1 - ti;
+    __syncthreads();
+  }
+}
+
 }  // namespace tnsp

@@ -14,7 +14,8 @@
 //
 // Sharing: all calls on a device use the same arena, and it keeps the contents of the last call.
 // Everything that must start at a known value (status word, the all-ones boundary element, site
-// metadata) is rewritten by every call before the kernel runs.  Two calls whose work overlaps on
+// metadata, the all-zero charges: this entry point treats every matrix as one block) is rewritten
+// by every call before the kernel runs.  Two calls whose work overlaps on
 // the GPU (different streams, or different host threads) race on the arena and give undefined
 // results: serialise them.
 //
@@ -92,15 +93,26 @@ extern "C" int tnsp_amplitude_noalloc(int L1, int L2, int P, const int* dims, co
   shape.Dmax = Dmax;
   Slots s{};
   plan_slots(&shape, s);
+  const long long chi = (long long)cut * Dmax;
+  if (chi > kMaxChi) return err(TNSP_E_TOO_LARGE, "cut * max bond extent exceeds 1024");
+  // arena layout: metadata, then one array per kind with an exact per-slot stride (the kernels
+  // index every per-slot array as base + blockIdx.x * stride)
   const size_t meta = align256(sizeof(int32_t))                      // status word
                       + align256(sizeof(double))                     // boundary "ones"
                       + align256(sizeof(int) * ns * 4)               // dims
-                      + align256(sizeof(long long) * ns);            // offsets
-  const size_t per_slot = align256((size_t)s.stride * sizeof(double)) + align256(sizeof(int) * 4 * kMaxL * kMaxL * 3) +
-                          align256(sizeof(int) * 4 * kMaxL) + align256(sizeof(int) * (size_t)cut * Dmax);
-  if (meta + per_slot > kNoAllocArenaBytes)
+                      + align256(sizeof(long long) * ns)             // offsets
+                      + align256(sizeof(int) * (size_t)ns * 4 * Dmax) // leg charges (zero)
+                      + align256(sizeof(int) * (size_t)P)            // physical charges (zero)
+                      + align256(sizeof(int) * (size_t)ns);          // site flux (zero)
+  const size_t scratch_slot = align256((size_t)s.stride * sizeof(double));
+  const size_t ints_slot = sizeof(int) * ((size_t)4 * kMaxL * kMaxL * 3 + 4 * kMaxL + (size_t)cut * Dmax +
+                                          (size_t)4 * kMaxL * kMaxL * 2 * cut + 4 * kMaxL * kMaxL +
+                                          (size_t)kMaxL * 3 * chi + kMaxL + (size_t)(chi * Dmax + chi));
+  const size_t per_slot = scratch_slot + ints_slot;
+  const size_t slack = 16 * 256;  // alignment of the eight per-slot arrays
+  if (meta + per_slot + slack > kNoAllocArenaBytes)
     return err(TNSP_E_TOO_LARGE, "one chain slot of this lattice/cut does not fit in the 64 MiB arena");
-  int nslots = (int)((kNoAllocArenaBytes - meta) / per_slot);
+  int nslots = (int)((kNoAllocArenaBytes - meta - slack) / per_slot);
   if (nslots > B) nslots = B;
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) == cudaSuccess &&
@@ -111,30 +123,40 @@ extern "C" int tnsp_amplitude_noalloc(int L1, int L2, int P, const int* dims, co
   cudaError_t e = arena_for_current_device(&base);
   if (e != cudaSuccess) return err(TNSP_E_CUDA, "cudaGetSymbolAddress failed");
   cudaStream_t st = (cudaStream_t)stream;
-  unsigned char* p = base;
-  int32_t* d_status = (int32_t*)p;
-  p += align256(sizeof(int32_t));
-  double* d_ones = (double*)p;
-  p += align256(sizeof(double));
-  int* d_dims = (int*)p;
-  p += align256(sizeof(int) * ns * 4);
-  long long* d_off = (long long*)p;
-  p += align256(sizeof(long long) * ns);
-  double* d_scratch = (double*)p;
-  p += align256((size_t)s.stride * sizeof(double)) * nslots;
-  s.ldims = (int*)p;
-  p += align256(sizeof(int) * 4 * kMaxL * kMaxL * 3) * nslots;
-  s.lexp = (int*)p;
-  p += align256(sizeof(int) * 4 * kMaxL) * nslots;
-  s.order = (int*)p;
-  // per-slot arrays are indexed with the kernel's own strides: make the carved strides match
-  // (stride in elements for scratch, fixed sizes for the integer arrays)
-  s.stride = (long long)(align256((size_t)s.stride * sizeof(double)) / sizeof(double));
+  size_t o = 0;
+  auto carve = [&](size_t bytes) {
+    o = align256(o);
+    unsigned char* r = base + o;
+    o += bytes;
+    return r;
+  };
+  int32_t* d_status = (int32_t*)carve(sizeof(int32_t));
+  double* d_ones = (double*)carve(sizeof(double));
+  int* d_dims = (int*)carve(sizeof(int) * ns * 4);
+  long long* d_off = (long long*)carve(sizeof(long long) * ns);
+  int* d_qleg = (int*)carve(sizeof(int) * (size_t)ns * 4 * Dmax);
+  int* d_qphys = (int*)carve(sizeof(int) * (size_t)P);
+  int* d_sflux = (int*)carve(sizeof(int) * (size_t)ns);
+  s.stride = (long long)(scratch_slot / sizeof(double));
+  double* d_scratch = (double*)carve(scratch_slot * nslots);
+  s.ldims = (int*)carve(sizeof(int) * 4 * kMaxL * kMaxL * 3 * (size_t)nslots);
+  s.lexp = (int*)carve(sizeof(int) * 4 * kMaxL * (size_t)nslots);
+  s.order = (int*)carve(sizeof(int) * (size_t)cut * Dmax * nslots);
+  s.lq = (int*)carve(sizeof(int) * (size_t)4 * kMaxL * kMaxL * 2 * cut * nslots);
+  s.lfl = (int*)carve(sizeof(int) * (size_t)4 * kMaxL * kMaxL * nslots);
+  s.tq = (int*)carve(sizeof(int) * (size_t)kMaxL * 3 * chi * nslots);
+  s.tfl = (int*)carve(sizeof(int) * (size_t)kMaxL * nslots);
+  s.ilist = (int*)carve(sizeof(int) * (size_t)(chi * Dmax + chi) * nslots);
+  s.smem_elems = 0;  // no dynamic shared memory: sector blocks are staged in the arena
+  if (o > kNoAllocArenaBytes) return err(TNSP_E_TOO_LARGE, "arena layout overflow");
   const double one = 1.0;
   if ((e = cudaMemsetAsync(d_status, 0, sizeof(int32_t), st)) != cudaSuccess ||
       (e = cudaMemcpyAsync(d_ones, &one, sizeof(double), cudaMemcpyHostToDevice, st)) != cudaSuccess ||
       (e = cudaMemcpyAsync(d_dims, dims, sizeof(int) * ns * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
-      (e = cudaMemcpyAsync(d_off, off_host, sizeof(long long) * ns, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+      (e = cudaMemcpyAsync(d_off, off_host, sizeof(long long) * ns, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+      (e = cudaMemsetAsync(d_qleg, 0, sizeof(int) * (size_t)ns * 4 * Dmax, st)) != cudaSuccess ||
+      (e = cudaMemsetAsync(d_qphys, 0, sizeof(int) * (size_t)P, st)) != cudaSuccess ||
+      (e = cudaMemsetAsync(d_sflux, 0, sizeof(int) * (size_t)ns, st)) != cudaSuccess)
     return err(TNSP_E_CUDA, "arena set-up copy failed");
   Model md{};
   md.L1 = L1;
@@ -146,6 +168,9 @@ extern "C" int tnsp_amplitude_noalloc(int L1, int L2, int P, const int* dims, co
   md.off = d_off;
   md.A = tensors;
   md.n_params = total;
+  md.qleg = d_qleg;
+  md.qphys = d_qphys;
+  md.sflux = d_sflux;
   amplitude_kernel<double><<<nslots, kThreads, 0, st>>>(md, s, d_scratch, d_ones, B, configs, mantissa, exponent,
                                                         d_status);
   if ((e = cudaGetLastError()) != cudaSuccess) return err(TNSP_E_CUDA, "kernel launch failed");

@@ -26,6 +26,8 @@ constexpr int kMaxL = 16;       // lattice extent limit (rows or columns)
 constexpr int kMaxSites = kMaxL * kMaxL;
 constexpr int kMtN = 312;
 constexpr int kMaxSweepsJacobi = 60;
+constexpr int kMaxSec = 96;     // charge sectors per factorised matrix
+constexpr int kMaxChi = 1024;   // cut * Dmax
 
 enum { ST_SVD_NOCONV = 1, ST_NONFINITE = 2, ST_UNSUPPORTED = 4, ST_ZERO_WS = 8 };
 enum { F_UP = 0, F_DOWN = 1, F_LEFT = 2, F_RIGHT = 3 };
@@ -45,6 +47,11 @@ struct Model {
   const int* tab_out;       // [entries]
   const double* tab_val;    // [entries]
   long long n_params;       // total elements of all site tensors
+  // charges (all zero without symmetry): every nonzero element of site tensor A[p][u][d][l][r]
+  // satisfies qphys[p] + qU[u] + qD[d] + qL[l] + qR[r] == sflux[site]
+  const int* qleg;          // [site][4][Dmax]: charge of each index of the U, D, L, R legs
+  const int* qphys;         // [P]
+  const int* sflux;         // [site]
 };
 
 struct Chains {
@@ -74,6 +81,12 @@ struct Slots {
   double* edelta;           // [slot][n_params]
   double* contrib;          // [slot][n_terms]
   double* flops;            // [slot][4]: algorithmic flops of contractions, QR, SVD, strip/hole work
+  int* lq;                  // [slot][4][kMaxL][kMaxL][2][cut]: charges of the left/right bond of line sites
+  int* lfl;                 // [slot][4][kMaxL][kMaxL]: flux of line sites
+  int* tq;                  // [slot][kMaxL][3][chi]: charges of the left/right/open legs of compression tensors
+  int* tfl;                 // [slot][kMaxL]
+  int* ilist;               // [slot][chi*Dmax + chi]: packed sector row lists, then column lists
+  long long smem_elems;     // dynamic shared memory available to a block, in elements of T
 };
 
 // ------------------------------------------------------------------------------------------
@@ -131,6 +144,8 @@ struct SiteView {  // a projected site tensor seen as W(u, d, l, r)
   long long base;
   int du, dd, dl, dr;
   int su, sd, sl, sr;
+  const int *qu, *qd, *ql, *qr;  // index charges of the four roles
+  int flux;                      // sum of the four leg charges of every nonzero element
 };
 
 struct Dims3 {
@@ -173,11 +188,14 @@ template <class T> struct Chain {
     const int sR = 1, sL = R, sD = L * R, sU = D * L * R;
     SiteView v;
     v.base = md.off[id] + (long long)s * U * D * L * R;
+    const int* q = md.qleg + (long long)id * 4 * md.Dmax;
+    const int *qU = q, *qD = q + md.Dmax, *qL = q + 2 * md.Dmax, *qR = q + 3 * md.Dmax;
+    v.flux = md.sflux[id] - md.qphys[s];
     switch (orient) {
-      case 0: v.du = U; v.su = sU; v.dd = D; v.sd = sD; v.dl = L; v.sl = sL; v.dr = R; v.sr = sR; break;
-      case 1: v.du = D; v.su = sD; v.dd = U; v.sd = sU; v.dl = L; v.sl = sL; v.dr = R; v.sr = sR; break;
-      case 2: v.du = L; v.su = sL; v.dd = R; v.sd = sR; v.dl = U; v.sl = sU; v.dr = D; v.sr = sD; break;
-      default: v.du = R; v.su = sR; v.dd = L; v.sd = sL; v.dl = U; v.sl = sU; v.dr = D; v.sr = sD; break;
+      case 0: v.du = U; v.su = sU; v.qu = qU; v.dd = D; v.sd = sD; v.qd = qD; v.dl = L; v.sl = sL; v.ql = qL; v.dr = R; v.sr = sR; v.qr = qR; break;
+      case 1: v.du = D; v.su = sD; v.qu = qD; v.dd = U; v.sd = sU; v.qd = qU; v.dl = L; v.sl = sL; v.ql = qL; v.dr = R; v.sr = sR; v.qr = qR; break;
+      case 2: v.du = L; v.su = sL; v.qu = qL; v.dd = R; v.sd = sR; v.qd = qR; v.dl = U; v.sl = sU; v.ql = qU; v.dr = D; v.sr = sD; v.qr = qD; break;
+      default: v.du = R; v.su = sR; v.qu = qR; v.dd = L; v.sd = sL; v.qd = qL; v.dl = U; v.sl = sU; v.ql = qU; v.dr = D; v.sr = sD; v.qr = qD; break;
     }
     return v;
   }
@@ -388,6 +406,12 @@ template <class T> struct Engine : Chain<T> {
   using Chain<T>::order;
   const T* ones;
   int32_t* status;
+  int* lq;
+  int* lfl;
+  int* tq;
+  int* tfl;
+  int* ilist;
+  T* smem;
   // strip currently held in E/F: kind 0 = row, 1 = column, -1 none
   int* strip_kind;
   int* strip_idx;
@@ -409,14 +433,89 @@ template <class T> struct Engine : Chain<T> {
 
   __device__ T* Tbuf(int k) const { return slot + sl.o_T + (long long)k * sl.capT; }
 
-  // _two_line_to_one_line for family f producing line idx (single_layer_auxiliaries.py:462-498)
+  // charges of line sites and of compression tensors
+  __device__ int* lqa(int f, int idx, int i) const {
+    return lq + ((((long long)f * kMaxL + idx) * kMaxL + i) * 2 + 0) * md.cut;
+  }
+  __device__ int* lqb(int f, int idx, int i) const {
+    return lq + ((((long long)f * kMaxL + idx) * kMaxL + i) * 2 + 1) * md.cut;
+  }
+  __device__ int* lflux(int f, int idx, int i) const { return lfl + ((long long)f * kMaxL + idx) * kMaxL + i; }
+  __device__ int chi() const { return md.cut * md.Dmax; }
+  __device__ int* tqL(int i) const { return tq + ((long long)i * 3 + 0) * chi(); }
+  __device__ int* tqR(int i) const { return tq + ((long long)i * 3 + 1) * chi(); }
+  __device__ int* tqD(int i) const { return tq + ((long long)i * 3 + 2) * chi(); }
+
+  // Sector table of a matrix whose rows carry charges qrow(x), columns qcol(z), and whose
+  // nonzeros satisfy qrow + qcol == F: one sector per row charge r (ascending) with matching
+  // columns F - r.  Row and column index lists are packed into ilist.
+  struct Sectors {
+    int n;
+    int r[kMaxSec], m[kMaxSec], c[kMaxSec], ro[kMaxSec], co[kMaxSec];
+  };
+
+  template <class QR, class QC>
+  __device__ void sectors(int rows, int cols, QR qrow, QC qcol, int F, Sectors* sec, int* sh) {
+    __shared__ int s_lo, s_hi;
+    if (threadIdx.x == 0) {
+      s_lo = 1 << 30;
+      s_hi = -(1 << 30);
+    }
+    __syncthreads();
+    int lo = 1 << 30, hi = -(1 << 30);
+    for (int x = threadIdx.x; x < rows; x += blockDim.x) {
+      const int q = qrow(x);
+      lo = q < lo ? q : lo;
+      hi = q > hi ? q : hi;
+    }
+    atomicMin(&s_lo, lo);
+    atomicMax(&s_hi, hi);
+    __syncthreads();
+    const int qlo = s_lo, qhi = s_hi;
+    int* rl = ilist;
+    int* cl = ilist + (long long)chi() * md.Dmax;
+    int nr = 0, nc = 0, ns = 0;
+    for (int q = qlo; q <= qhi; ++q) {
+      const int mr = block_compact(rows, [&](int x) { return qrow(x) == q; }, rl + nr, sh);
+      if (mr == 0) continue;
+      const int mc = block_compact(cols, [&](int z) { return qcol(z) == F - q; }, cl + nc, sh);
+      if (mc == 0) continue;
+      if (ns >= kMaxSec) {
+        if (threadIdx.x == 0) atomicOr(status, ST_UNSUPPORTED);
+        break;
+      }
+      if (threadIdx.x == 0) {
+        sec->r[ns] = q;
+        sec->m[ns] = mr;
+        sec->c[ns] = mc;
+        sec->ro[ns] = nr;
+        sec->co[ns] = nc;
+      }
+      nr += mr;
+      nc += mc;
+      ++ns;
+    }
+    if (threadIdx.x == 0) sec->n = ns;
+    __syncthreads();
+  }
+
+  // _two_line_to_one_line for family f producing line idx (single_layer_auxiliaries.py:462-498).
+  // Every QR and SVD is done per charge sector (TAT/include/TAT/implement/qr.hpp:310-510,
+  // svd.hpp:259-532); the SVD truncation keeps the `cut` largest singular values over all
+  // sectors (svd.hpp:429-470).  Without symmetry every charge is zero: one sector.
   __device__ void compress(int f, int idx) {
     const int n = nsites_along(f);
     const int prev = (f == F_UP || f == F_LEFT) ? idx - 1 : idx + 1;
     const int orient = f;  // 0: UDLR, 1: DULR, 2: LRUD, 3: RLUD
     __shared__ int s_buf[kMaxL + 2];
-    __shared__ int s_dA[kMaxL], s_dd[kMaxL], s_dB[kMaxL];
-    // slot buffers: T pool has n + 2 buffers; s_buf maps site -> buffer
+    __shared__ int s_dA[kMaxL], s_dd[kMaxL], s_dB[kMaxL], s_fl[kMaxL];
+    __shared__ int s_sh[kWarps + 1];
+    __shared__ Sectors s_sec;
+    __shared__ short s_kmap[kMaxChi];  // new bond index -> sector
+    __shared__ short s_kloc[kMaxChi];  // new bond index -> local index in its sector
+    __shared__ int s_roffs[kMaxSec];
+    __shared__ int s_xo[kMaxSec], s_vo[kMaxSec], s_so[kMaxSec];
+    const bool ones_prev = is_ones(f, prev);
     if (threadIdx.x < n + 2) s_buf[threadIdx.x] = threadIdx.x;
     __syncthreads();
     int expo = lexpo(f, prev);
@@ -426,153 +525,300 @@ template <class T> struct Engine : Chain<T> {
       const Dims3 ld = lsdim(f, prev, i);
       two_line(lsite(f, prev, i), ld, A, w, Tbuf(s_buf[i]));
       this->count(0, 2.0 * ld.a * w.dl * w.dd * ld.b * w.dr * ld.p);
+      const int* qa = ones_prev ? nullptr : lqa(f, prev, i);
+      const int* qb = ones_prev ? nullptr : lqb(f, prev, i);
+      int* L = tqL(i);
+      int* Rr = tqR(i);
+      int* Dd = tqD(i);
+      for (int x = threadIdx.x; x < ld.a * w.dl; x += blockDim.x) L[x] = (qa ? qa[x / w.dl] : 0) + w.ql[x % w.dl];
+      for (int z = threadIdx.x; z < ld.b * w.dr; z += blockDim.x) Rr[z] = (qb ? qb[z / w.dr] : 0) + w.qr[z % w.dr];
+      for (int d = threadIdx.x; d < w.dd; d += blockDim.x) Dd[d] = w.qd[d];
       if (threadIdx.x == 0) {
         s_dA[i] = ld.a * w.dl;
         s_dd[i] = w.dd;
         s_dB[i] = ld.b * w.dr;
+        s_fl[i] = (ones_prev ? 0 : *lflux(f, prev, i)) + w.flux;
       }
       __syncthreads();
     }
-    T* R = slot + sl.o_R;
+    T* Rb = slot + sl.o_R;
     T* tau = slot + sl.o_tau;
-    // QR sweep
+    T* sm = smem;
+    const long long smcap = sl.smem_elems;
+    int* rl = ilist;
+    int* cl = ilist + (long long)chi() * md.Dmax;
+    // ---------------- QR sweep, per sector ----------------
     for (int i = 0; i < n - 1; ++i) {
-      const int rows = s_dA[i] * s_dd[i], cols = s_dB[i];
-      const int kk = rows < cols ? rows : cols;
-      const int spare = s_buf[n];
-      block_qr(rows, cols, Tbuf(s_buf[i]), Tbuf(spare), R, tau, red);
+      const int d = s_dd[i], rows = s_dA[i] * d, cols = s_dB[i], F = s_fl[i];
+      const int* qL = tqL(i);
+      const int* qD = tqD(i);
+      const int* qR = tqR(i);
+      sectors(rows, cols, [&](int x) { return qL[x / d] + qD[x % d]; }, [&](int z) { return qR[z]; }, F, &s_sec, s_sh);
+      const int ns = s_sec.n;
+      int ktot = 0;
+      for (int t = 0; t < ns; ++t) ktot += min(s_sec.m[t], s_sec.c[t]);
+      const int spare = s_buf[n], spare2 = s_buf[n + 1];
+      T* Tq = Tbuf(spare);  // new T[i] = Q (rows x ktot)
+      T* G = Tbuf(spare2);  // sector staging, later new T[i+1]
+      for (long long t = threadIdx.x; t < (long long)rows * ktot; t += blockDim.x) Tq[t] = (T)0;
+      if (threadIdx.x == 0) {
+        int o = 0;
+        for (int t = 0; t < ns; ++t) {
+          s_roffs[t] = o;
+          o += min(s_sec.m[t], s_sec.c[t]) * s_sec.c[t];
+        }
+      }
+      __syncthreads();
+      int koff = 0;
+      double rsz = 0;
+      for (int t = 0; t < ns; ++t) {
+        const int mr = s_sec.m[t], mc = s_sec.c[t], kr = min(mr, mc);
+        const int* R_ = rl + s_sec.ro[t];
+        const int* C_ = cl + s_sec.co[t];
+        const T* M = Tbuf(s_buf[i]);
+        T* g = ((long long)mr * mc <= smcap) ? sm : G;
+        for (long long e = threadIdx.x; e < (long long)mr * mc; e += blockDim.x) {
+          const int y = (int)(e / mr), x = (int)(e % mr);
+          g[e] = M[(long long)R_[x] * cols + C_[y]];
+        }
+        __syncthreads();
+        block_geqrf_cm(mr, mc, g, tau, red);
+        {
+          const double mm = mr > mc ? mr : mc, nn = kr;
+          this->count(1, 2.0 * (2.0 * mm * nn * nn - 2.0 * nn * nn * nn / 3.0));
+        }
+        // R (kr x mc, row-major) into Rb
+        T* rb = Rb + s_roffs[t];
+        for (long long e = threadIdx.x; e < (long long)kr * mc; e += blockDim.x) {
+          const int y = (int)(e / mc), z = (int)(e % mc);
+          rb[e] = z >= y ? g[(long long)z * mr + y] : (T)0;
+        }
+        __syncthreads();
+        block_orgqr_cm(mr, kr, g, tau);
+        for (long long e = threadIdx.x; e < (long long)mr * kr; e += blockDim.x) {
+          const int y = (int)(e / mr), x = (int)(e % mr);
+          Tq[(long long)R_[x] * ktot + koff + y] = g[e];
+        }
+        for (int y = threadIdx.x; y < kr; y += blockDim.x) {
+          s_kmap[koff + y] = (short)t;
+          s_kloc[koff + y] = (short)y;
+        }
+        __syncthreads();
+        koff += kr;
+        rsz += (double)kr * mc;
+      }
+      // new T[i+1] (ktot x d'B') = R * T[i+1], sector by sector, into G
+      const int dB = s_dd[i + 1] * s_dB[i + 1];
       {
-        const double mm = rows > cols ? rows : cols, nn = kk;
-        this->count(1, 2.0 * (2.0 * mm * nn * nn - 2.0 * nn * nn * nn / 3.0));
+        const T* Tn = Tbuf(s_buf[i + 1]);
+        for (long long e = threadIdx.x; e < (long long)ktot * dB; e += blockDim.x) {
+          const int k = (int)(e / dB), col = (int)(e % dB);
+          const int t = s_kmap[k], y = s_kloc[k], mc = s_sec.c[t];
+          const T* rr = Rb + s_roffs[t] + (long long)y * mc;
+          const int* C_ = cl + s_sec.co[t];
+          T acc = 0;
+          for (int z = y; z < mc; ++z) acc = fma(rr[z], Tn[(long long)C_[z] * dB + col], acc);
+          G[e] = acc;
+        }
+        this->count(0, 2.0 * dB * rsz);
       }
+      __syncthreads();
+      // charges and flux of the new bond: Q side -r, R side +r
+      {
+        int* qRi = tqR(i);
+        int* qLn = tqL(i + 1);
+        for (int k = threadIdx.x; k < ktot; k += blockDim.x) {
+          const int r = s_sec.r[s_kmap[k]];
+          qRi[k] = -r;
+          qLn[k] = r;
+        }
+      }
+      __syncthreads();
       if (threadIdx.x == 0) {
-        s_buf[n] = s_buf[i];
+        const int old_i = s_buf[i], old_n = s_buf[i + 1];
         s_buf[i] = spare;
-        s_dB[i] = kk;
-      }
-      __syncthreads();
-      // T[i+1] <- R * T[i+1]
-      const int spare2 = s_buf[n];
-      block_gemm(kk, s_dd[i + 1] * s_dB[i + 1], cols, R, cols, Tbuf(s_buf[i + 1]), s_dd[i + 1] * s_dB[i + 1],
-                 Tbuf(spare2), s_dd[i + 1] * s_dB[i + 1]);
-      this->count(0, 2.0 * kk * cols * s_dd[i + 1] * s_dB[i + 1]);
-      if (threadIdx.x == 0) {
-        s_buf[n] = s_buf[i + 1];
         s_buf[i + 1] = spare2;
-        s_dA[i + 1] = kk;
+        s_buf[n] = old_i;
+        s_buf[n + 1] = old_n;
+        s_dB[i] = ktot;
+        s_dA[i + 1] = ktot;
+        s_fl[i + 1] += s_fl[i];
+        s_fl[i] = 0;
       }
       __syncthreads();
-      expo += block_normalize(Tbuf(s_buf[i + 1]), (long long)kk * s_dd[i + 1] * s_dB[i + 1], red);
+      expo += block_normalize(Tbuf(s_buf[i + 1]), (long long)ktot * dB, red);
     }
-    // SVD sweep with truncation
+    // ---------------- truncating SVD sweep, per sector, global cut ----------------
     T* X = slot + sl.o_X;
     T* V = slot + sl.o_V;
     T* sig = slot + sl.o_sig;
     for (int i = n - 1; i >= 1; --i) {
-      const int rows = s_dA[i], cols = s_dd[i] * s_dB[i];
-      const T* M = Tbuf(s_buf[i]);
-      const bool caseA = cols <= rows;
-      const int nv = caseA ? cols : rows, len = caseA ? rows : cols;
-      if (caseA) {
-        for (long long t = threadIdx.x; t < (long long)nv * len; t += blockDim.x) {
-          const int j = (int)(t / len), r = (int)(t % len);
-          X[t] = M[(long long)r * cols + j];
+      const int d = s_dd[i], Bc = s_dB[i], rows = s_dA[i], cols = d * Bc, F = s_fl[i];
+      const int* qL = tqL(i);
+      const int* qD = tqD(i);
+      const int* qR = tqR(i);
+      sectors(rows, cols, [&](int x) { return qL[x]; }, [&](int z) { return qD[z / Bc] + qR[z % Bc]; }, F, &s_sec,
+              s_sh);
+      const int ns = s_sec.n;
+      if (threadIdx.x == 0) {
+        int xo = 0, vo = 0, so = 0;
+        for (int t = 0; t < ns; ++t) {
+          const int nv = min(s_sec.m[t], s_sec.c[t]), len = max(s_sec.m[t], s_sec.c[t]);
+          s_xo[t] = xo;
+          s_vo[t] = vo;
+          s_so[t] = so;
+          xo += nv * len;
+          vo += nv * nv;
+          so += nv;
         }
-      } else {
-        for (long long t = threadIdx.x; t < (long long)nv * len; t += blockDim.x) X[t] = M[t];
       }
       __syncthreads();
-      const int sweeps = block_jacobi(nv, len, X, V, kMaxSweepsJacobi);
-      {
-        const double mm = len, nn = nv;
-        this->count(2, 4.0 * mm * mm * nn + 8.0 * mm * nn * nn + 9.0 * nn * nn * nn);
-      }
-      if (sweeps < 0 && threadIdx.x == 0) atomicOr(status, ST_SVD_NOCONV);
-      // singular values
-      {
+      int S = 0;
+      for (int t = 0; t < ns; ++t) S += min(s_sec.m[t], s_sec.c[t]);
+      const T* M = Tbuf(s_buf[i]);
+      for (int t = 0; t < ns; ++t) {
+        const int mr = s_sec.m[t], mc = s_sec.c[t];
+        const bool caseA = mc <= mr;
+        const int nv = caseA ? mc : mr, len = caseA ? mr : mc;
+        const int* R_ = rl + s_sec.ro[t];
+        const int* C_ = cl + s_sec.co[t];
+        const bool in_smem = (long long)nv * len + (long long)nv * nv <= smcap;
+        T* x = in_smem ? sm : X + s_xo[t];
+        T* v = in_smem ? sm + (long long)nv * len : V + s_vo[t];
+        for (long long e = threadIdx.x; e < (long long)nv * len; e += blockDim.x) {
+          const int j = (int)(e / len), q = (int)(e % len);
+          x[e] = caseA ? M[(long long)R_[q] * cols + C_[j]] : M[(long long)R_[j] * cols + C_[q]];
+        }
+        __syncthreads();
+        const int sweeps = block_jacobi(nv, len, x, v, kMaxSweepsJacobi);
+        if (sweeps < 0 && threadIdx.x == 0) atomicOr(status, ST_SVD_NOCONV);
+        {
+          const double mm = len, nn = nv;
+          this->count(2, 4.0 * mm * mm * nn + 8.0 * mm * nn * nn + 9.0 * nn * nn * nn);
+        }
         const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
         for (int j = wp; j < nv; j += kWarps) {
           T s2 = 0;
-          for (int r = lane; r < len; r += 32) s2 = fma(X[(long long)j * len + r], X[(long long)j * len + r], s2);
+          for (int q = lane; q < len; q += 32) s2 = fma(x[(long long)j * len + q], x[(long long)j * len + q], s2);
           s2 = warp_sum(s2);
-          if (lane == 0) sig[j] = sqrt(s2);
+          if (lane == 0) sig[s_so[t] + j] = sqrt(s2);
         }
+        if (in_smem) {
+          for (long long e = threadIdx.x; e < (long long)nv * len; e += blockDim.x) X[s_xo[t] + e] = x[e];
+          for (long long e = threadIdx.x; e < (long long)nv * nv; e += blockDim.x) V[s_vo[t] + e] = v[e];
+        }
+        __syncthreads();
       }
-      __syncthreads();
-      const int c = md.cut < nv ? md.cut : nv;
-      // rank selection: descending, ties by index
-      for (int j = threadIdx.x; j < nv; j += blockDim.x) {
+      const int c = md.cut < S ? md.cut : S;
+      // global selection: descending value, ties to the earlier sector / lower index
+      for (int j = threadIdx.x; j < S; j += blockDim.x) {
         const T sj = sig[j];
         int rank = 0;
-        for (int k = 0; k < nv; ++k) {
+        for (int k = 0; k < S; ++k) {
           const T sk = sig[k];
           rank += (sk > sj) || (sk == sj && k < j);
         }
         if (rank < c) order[rank] = j;
       }
       __syncthreads();
+      // kept index -> (sector, local)
+      for (int k = threadIdx.x; k < c; k += blockDim.x) {
+        const int j = order[k];
+        int t = 0;
+        while (t + 1 < ns && s_so[t + 1] <= j) ++t;
+        s_kmap[k] = (short)t;
+        s_kloc[k] = (short)(j - s_so[t]);
+      }
       T smax = 0;
-      for (int j = threadIdx.x; j < nv; j += blockDim.x) smax = fmax(smax, sig[j]);
+      for (int j = threadIdx.x; j < S; j += blockDim.x) smax = fmax(smax, sig[j]);
       smax = block_max(smax, red);
-      const T thr = smax * Eps<T>::value() * (T)len;
-      // new T[i] (c x cols) into spare, US (rows x c) into R
-      const int spare = s_buf[n];
-      T* Tn = Tbuf(spare);
-      for (long long t = threadIdx.x; t < (long long)c * cols; t += blockDim.x) {
-        const int tr = (int)(t / cols), q = (int)(t % cols);
-        const int j = order[tr];
-        T v;
-        if (caseA) {
-          v = V[(long long)j * nv + q];
-        } else {
-          const T s = sig[j];
-          v = s > thr ? X[(long long)j * len + q] / s : (T)0;
+      int lmaxi = 1;
+      for (int t = 0; t < ns; ++t) lmaxi = max(lmaxi, max(s_sec.m[t], s_sec.c[t]));
+      const T thr = smax * Eps<T>::value() * (T)lmaxi;
+      const int spare = s_buf[n], spare2 = s_buf[n + 1];
+      T* Tn = Tbuf(spare);  // new T[i] (c x cols)
+      for (long long e = threadIdx.x; e < (long long)c * cols; e += blockDim.x) Tn[e] = (T)0;
+      for (long long e = threadIdx.x; e < (long long)rows * c; e += blockDim.x) Rb[e] = (T)0;
+      __syncthreads();
+      const int span = max(rows, cols);
+      for (long long e = threadIdx.x; e < (long long)c * span; e += blockDim.x) {
+        const int k = (int)(e / span), q = (int)(e % span);
+        const int t = s_kmap[k], j = s_kloc[k];
+        const int mr = s_sec.m[t], mc = s_sec.c[t];
+        const bool caseA = mc <= mr;
+        const int nv = caseA ? mc : mr, len = caseA ? mr : mc;
+        const T sv = sig[s_so[t] + j];
+        const T* xj = X + s_xo[t] + (long long)j * len;
+        const T* vj = V + s_vo[t] + (long long)j * nv;
+        if (q < mc) {  // right singular vector component at column C[q]
+          const T val = caseA ? vj[q] : (sv > thr ? xj[q] / sv : (T)0);
+          Tn[(long long)k * cols + cl[s_sec.co[t] + q]] = val;
         }
-        Tn[t] = v;
+        if (q < mr) {  // U*S component at row R[q]
+          const T val = caseA ? xj[q] : (sv > thr ? vj[q] * sv : (T)0);
+          Rb[(long long)rl[s_sec.ro[t] + q] * c + k] = val;
+        }
       }
-      for (long long t = threadIdx.x; t < (long long)rows * c; t += blockDim.x) {
-        const int r = (int)(t / c), tr = (int)(t % c);
-        const int j = order[tr];
-        T v;
-        if (caseA) {
-          v = X[(long long)j * len + r];
-        } else {
-          const T s = sig[j];
-          v = s > thr ? V[(long long)j * nv + r] * s : (T)0;
+      __syncthreads();
+      // new T[i-1] (A d x c) = T[i-1] * US, summing only over the rows of each kept vector's sector
+      {
+        const int Ad = s_dA[i - 1] * s_dd[i - 1];
+        const T* Tp = Tbuf(s_buf[i - 1]);
+        T* out = Tbuf(spare2);
+        for (long long e = threadIdx.x; e < (long long)Ad * c; e += blockDim.x) {
+          const int xr = (int)(e / c), k = (int)(e % c);
+          const int t = s_kmap[k];
+          const int* R_ = rl + s_sec.ro[t];
+          const int mr = s_sec.m[t];
+          T acc = 0;
+          for (int q = 0; q < mr; ++q) acc = fma(Tp[(long long)xr * rows + R_[q]], Rb[(long long)R_[q] * c + k], acc);
+          out[e] = acc;
         }
-        R[t] = v;
+        double fl = 0;
+        for (int k = 0; k < c; ++k) fl += 2.0 * Ad * s_sec.m[s_kmap[k]];
+        this->count(0, fl);
+      }
+      {
+        int* qLi = tqL(i);
+        int* qRp = tqR(i - 1);
+        for (int k = threadIdx.x; k < c; k += blockDim.x) {
+          const int r = s_sec.r[s_kmap[k]];
+          qLi[k] = r;
+          qRp[k] = -r;
+        }
       }
       __syncthreads();
       if (threadIdx.x == 0) {
-        s_buf[n] = s_buf[i];
+        const int old_i = s_buf[i], old_p = s_buf[i - 1];
         s_buf[i] = spare;
-        s_dA[i] = c;
-      }
-      __syncthreads();
-      // T[i-1] <- T[i-1] * US
-      const int spare2 = s_buf[n];
-      block_gemm(s_dA[i - 1] * s_dd[i - 1], c, rows, Tbuf(s_buf[i - 1]), rows, R, c, Tbuf(spare2), c);
-      this->count(0, 2.0 * s_dA[i - 1] * s_dd[i - 1] * rows * c);
-      if (threadIdx.x == 0) {
-        s_buf[n] = s_buf[i - 1];
         s_buf[i - 1] = spare2;
+        s_buf[n] = old_i;
+        s_buf[n + 1] = old_p;
+        s_dA[i] = c;
         s_dB[i - 1] = c;
       }
       __syncthreads();
       expo += block_normalize(Tbuf(s_buf[i - 1]), (long long)s_dA[i - 1] * s_dd[i - 1] * c, red);
     }
     if (n == 1) expo += block_normalize(Tbuf(s_buf[0]), (long long)s_dA[0] * s_dd[0] * s_dB[0], red);
-    // store the line
+    // store the line with its charges
     for (int i = 0; i < n; ++i) {
       const long long cnt = (long long)s_dA[i] * s_dd[i] * s_dB[i];
       const T* src = Tbuf(s_buf[i]);
       T* dst = line(f, idx, i);
       for (long long t = threadIdx.x; t < cnt; t += blockDim.x) dst[t] = src[t];
+      int* qa = lqa(f, idx, i);
+      int* qb = lqb(f, idx, i);
+      const int* sa = tqL(i);
+      const int* sb = tqR(i);
+      for (int x = threadIdx.x; x < s_dA[i]; x += blockDim.x) qa[x] = sa[x];
+      for (int x = threadIdx.x; x < s_dB[i]; x += blockDim.x) qb[x] = sb[x];
       if (threadIdx.x == 0) {
-        int* d = ldim(f, idx, i);
-        d[0] = s_dA[i];
-        d[1] = s_dd[i];
-        d[2] = s_dB[i];
+        int* dd = ldim(f, idx, i);
+        dd[0] = s_dA[i];
+        dd[1] = s_dd[i];
+        dd[2] = s_dB[i];
+        *lflux(f, idx, i) = s_fl[i];
       }
     }
     if (threadIdx.x == 0) lexp[f * kMaxL + idx] = expo;
@@ -746,6 +992,18 @@ template <class T> struct Engine : Chain<T> {
   }
 };
 
+// per-slot integer arrays and the dynamic shared-memory staging area of this block
+template <class T> __device__ void bind_slot(Engine<T>& eng, const Slots& sl, const Model& md) {
+  extern __shared__ __align__(16) unsigned char dyn_smem[];
+  const long long chi = (long long)md.cut * md.Dmax;
+  eng.lq = sl.lq + (long long)blockIdx.x * 4 * kMaxL * kMaxL * 2 * md.cut;
+  eng.lfl = sl.lfl + (long long)blockIdx.x * 4 * kMaxL * kMaxL;
+  eng.tq = sl.tq + (long long)blockIdx.x * kMaxL * 3 * chi;
+  eng.tfl = sl.tfl + (long long)blockIdx.x * kMaxL;
+  eng.ilist = sl.ilist + (long long)blockIdx.x * (chi * md.Dmax + chi);
+  eng.smem = reinterpret_cast<T*>(dyn_smem);
+}
+
 __device__ __forceinline__ double ratio_of(double m1, int e1, double m0, int e0) {
   return ldexp(m1 / m0, e1 - e0);
 }
@@ -855,7 +1113,12 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Sl
   Engine<T> eng{{md, sl, scratch + (long long)blockIdx.x * sl.stride, (const T*)md.A,
                  sl.ldims + (long long)blockIdx.x * 4 * kMaxL * kMaxL * 3, sl.lexp + (long long)blockIdx.x * 4 * kMaxL,
                  sl.order + (long long)blockIdx.x * md.cut * md.Dmax, s_conf, s_valid, s_eE, s_eF, s_red, s_dred, s_fl},
-                ones, ch.status, &s_strip_kind, &s_strip_idx, &s_strip_eupto, &s_strip_ffrom};
+                ones, ch.status};
+  eng.strip_kind = &s_strip_kind;
+  eng.strip_idx = &s_strip_idx;
+  eng.strip_eupto = &s_strip_eupto;
+  eng.strip_ffrom = &s_strip_ffrom;
+  bind_slot(eng, sl, md);
   double* delta = sl.delta + (long long)blockIdx.x * md.n_params;
   double* edelta = sl.edelta + (long long)blockIdx.x * md.n_params;
   double* contrib = sl.contrib + (long long)blockIdx.x * md.n_terms;
@@ -1056,7 +1319,12 @@ __global__ void __launch_bounds__(kThreads) amplitude_kernel(Model md, Slots sl,
   Engine<T> eng{{md, sl, scratch + (long long)blockIdx.x * sl.stride, (const T*)md.A,
                  sl.ldims + (long long)blockIdx.x * 4 * kMaxL * kMaxL * 3, sl.lexp + (long long)blockIdx.x * 4 * kMaxL,
                  sl.order + (long long)blockIdx.x * md.cut * md.Dmax, s_conf, s_valid, s_eE, s_eF, s_red, s_dred, s_fl},
-                ones, status, &s_strip_kind, &s_strip_idx, &s_strip_eupto, &s_strip_ffrom};
+                ones, status};
+  eng.strip_kind = &s_strip_kind;
+  eng.strip_idx = &s_strip_idx;
+  eng.strip_eupto = &s_strip_eupto;
+  eng.strip_ffrom = &s_strip_ffrom;
+  bind_slot(eng, sl, md);
   for (int b = blockIdx.x; b < B; b += gridDim.x) {
     for (int i = threadIdx.x; i < nsite; i += blockDim.x) s_conf[i] = (short)confs[(long long)b * nsite + i];
     for (int i = threadIdx.x; i < 4 * kMaxL; i += blockDim.x) s_valid[i] = 0;

@@ -28,6 +28,11 @@ struct tnsp_ctx {
   float* dA32 = nullptr;
   int* d_dims = nullptr;
   long long* d_off = nullptr;
+  std::vector<double> hostA;       // host copy of the site tensors (charge validation)
+  int* d_qleg = nullptr;           // [site][4][Dmax]
+  int* d_qphys = nullptr;          // [P]
+  int* d_sflux = nullptr;          // [site]
+  bool charged = false;
   // model
   int n_terms = 0;
   int* d_term_sites = nullptr;
@@ -64,6 +69,12 @@ struct tnsp_ctx {
   double* d_contrib = nullptr;
   double* d_red = nullptr;
   double* d_flops = nullptr;
+  int* d_lq = nullptr;
+  int* d_lfl = nullptr;
+  int* d_tq = nullptr;
+  int* d_tfl = nullptr;
+  int* d_ilist = nullptr;
+  size_t smem_bytes = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0;
   long long last_launches = 0;
@@ -99,6 +110,11 @@ void free_slots(tnsp_ctx* c) {
   dfree(c->d_contrib);
   dfree(c->d_red);
   dfree(c->d_flops);
+  dfree(c->d_lq);
+  dfree(c->d_lfl);
+  dfree(c->d_tq);
+  dfree(c->d_tfl);
+  dfree(c->d_ilist);
   c->nslots = 0;
 }
 
@@ -133,6 +149,9 @@ void free_lattice(tnsp_ctx* c) {
   dfree(c->dA32);
   dfree(c->d_dims);
   dfree(c->d_off);
+  dfree(c->d_qleg);
+  dfree(c->d_qphys);
+  dfree(c->d_sflux);
   c->has_lattice = false;
 }
 
@@ -156,6 +175,9 @@ Model make_model(tnsp_ctx* c) {
   m.tab_out = c->d_tab_out;
   m.tab_val = c->d_tab_val;
   m.n_params = c->n_params;
+  m.qleg = c->d_qleg;
+  m.qphys = c->d_qphys;
+  m.sflux = c->d_sflux;
   return m;
 }
 
@@ -238,6 +260,23 @@ int ensure_slots(tnsp_ctx* ctx) {
   CK(cudaMalloc((void**)&ctx->d_contrib, sizeof(double) * std::max(1, ctx->n_terms) * ctx->nslots));
   CK(cudaMalloc((void**)&ctx->d_red, sizeof(double) * ctx->n_params * 2));
   CK(cudaMalloc((void**)&ctx->d_flops, sizeof(double) * 4 * ctx->nslots));
+  {
+    const long long chi = (long long)ctx->cut * ctx->Dmax;
+    CK(cudaMalloc((void**)&ctx->d_lq, sizeof(int) * 4 * kMaxL * kMaxL * 2 * ctx->cut * ctx->nslots));
+    CK(cudaMalloc((void**)&ctx->d_lfl, sizeof(int) * 4 * kMaxL * kMaxL * ctx->nslots));
+    CK(cudaMalloc((void**)&ctx->d_tq, sizeof(int) * kMaxL * 3 * chi * ctx->nslots));
+    CK(cudaMalloc((void**)&ctx->d_tfl, sizeof(int) * kMaxL * ctx->nslots));
+    CK(cudaMalloc((void**)&ctx->d_ilist, sizeof(int) * (chi * ctx->Dmax + chi) * ctx->nslots));
+  }
+  // dynamic shared memory for sector staging: 96 KB keeps two blocks per SM
+  ctx->smem_bytes = 96 * 1024;
+  if (ctx->precision == TNSP_FP64) {
+    CK(cudaFuncSetAttribute(sweep_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_bytes));
+    CK(cudaFuncSetAttribute(amplitude_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_bytes));
+  } else {
+    CK(cudaFuncSetAttribute(sweep_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_bytes));
+    CK(cudaFuncSetAttribute(amplitude_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_bytes));
+  }
   CK(cudaMemsetAsync(ctx->d_flops, 0, sizeof(double) * 4 * ctx->nslots, ctx->stream));
   CK(cudaMemsetAsync(ctx->d_delta, 0, sizeof(double) * ctx->n_params * ctx->nslots, ctx->stream));
   CK(cudaMemsetAsync(ctx->d_edelta, 0, sizeof(double) * ctx->n_params * ctx->nslots, ctx->stream));
@@ -253,6 +292,12 @@ int ensure_slots(tnsp_ctx* ctx) {
   s.edelta = ctx->d_edelta;
   s.contrib = ctx->d_contrib;
   s.flops = ctx->d_flops;
+  s.lq = ctx->d_lq;
+  s.lfl = ctx->d_lfl;
+  s.tq = ctx->d_tq;
+  s.tfl = ctx->d_tfl;
+  s.ilist = ctx->d_ilist;
+  s.smem_elems = (long long)(ctx->smem_bytes / ctx->elem);
   ctx->slots = s;
   return 0;
 }
@@ -351,6 +396,7 @@ int tnsp_lattice_upload(tnsp_ctx* ctx, int L1, int L2, int P, const int* dims, c
     }
   for (long long i = 0; i < total; ++i)
     if (!std::isfinite(tensors[i])) return fail(ctx, TNSP_E_ARG, "non-finite element in the site tensors");
+  if ((long long)cut * Dmax > kMaxChi) return fail(ctx, TNSP_E_ARG, "cut * max bond extent exceeds 1024");
   const bool reshape = ctx->has_lattice && (L1 != ctx->L1 || L2 != ctx->L2 || P != ctx->P || cut != ctx->cut ||
                                             Dmax != ctx->Dmax || dv != ctx->dims);
   if (reshape) {
@@ -364,7 +410,15 @@ int tnsp_lattice_upload(tnsp_ctx* ctx, int L1, int L2, int P, const int* dims, c
     CK(cudaMalloc((void**)&ctx->dA32, sizeof(float) * total));
     CK(cudaMalloc((void**)&ctx->d_dims, sizeof(int) * dv.size()));
     CK(cudaMalloc((void**)&ctx->d_off, sizeof(long long) * off.size()));
+    CK(cudaMalloc((void**)&ctx->d_qleg, sizeof(int) * (size_t)L1 * L2 * 4 * Dmax));
+    CK(cudaMalloc((void**)&ctx->d_qphys, sizeof(int) * P));
+    CK(cudaMalloc((void**)&ctx->d_sflux, sizeof(int) * (size_t)L1 * L2));
+    CK(cudaMemset(ctx->d_qleg, 0, sizeof(int) * (size_t)L1 * L2 * 4 * Dmax));
+    CK(cudaMemset(ctx->d_qphys, 0, sizeof(int) * P));
+    CK(cudaMemset(ctx->d_sflux, 0, sizeof(int) * (size_t)L1 * L2));
+    ctx->charged = false;
   }
+  ctx->hostA.assign(tensors, tensors + total);
   std::vector<float> a32(tensors, tensors + total);
   CK(cudaMemcpyAsync(ctx->dA64, tensors, sizeof(double) * total, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->dA32, a32.data(), sizeof(float) * total, cudaMemcpyHostToDevice, ctx->stream));
@@ -380,6 +434,54 @@ int tnsp_lattice_upload(tnsp_ctx* ctx, int L1, int L2, int P, const int* dims, c
   ctx->off = off;
   ctx->n_params = total;
   ctx->has_lattice = true;
+  return TNSP_OK;
+}
+
+int tnsp_lattice_charges(tnsp_ctx* ctx, const int* leg_charges, const int* phys_charges, const int* site_flux) {
+  if (!ctx) return TNSP_E_ARG;
+  if (!ctx->has_lattice) return fail(ctx, TNSP_E_STATE, "upload the lattice first");
+  if (!leg_charges || !phys_charges || !site_flux) return fail(ctx, TNSP_E_ARG, "null charge array");
+  CK(cudaSetDevice(ctx->device));
+  const int L1 = ctx->L1, L2 = ctx->L2, P = ctx->P, Dm = ctx->Dmax;
+  // every nonzero element must conserve charge, otherwise the sector factorisation would drop it
+  for (int id = 0; id < L1 * L2; ++id) {
+    const int* d = &ctx->dims[id * 4];
+    const int* q = leg_charges + (size_t)id * 4 * Dm;
+    const double* a = ctx->hostA.data() + ctx->off[id];
+    long long e = 0;
+    for (int p = 0; p < P; ++p)
+      for (int u = 0; u < d[0]; ++u)
+        for (int dd = 0; dd < d[1]; ++dd)
+          for (int l = 0; l < d[2]; ++l)
+            for (int r = 0; r < d[3]; ++r, ++e)
+              if (a[e] != 0.0 &&
+                  phys_charges[p] + q[u] + q[Dm + dd] + q[2 * Dm + l] + q[3 * Dm + r] != site_flux[id]) {
+                char buf[160];
+                snprintf(buf, sizeof buf, "site %d: element (%d,%d,%d,%d,%d) violates charge conservation", id, p, u,
+                         dd, l, r);
+                return fail(ctx, TNSP_E_ARG, buf);
+              }
+  }
+  // bonds must carry opposite charges on their two ends
+  for (int l1 = 0; l1 < L1; ++l1)
+    for (int l2 = 0; l2 < L2; ++l2) {
+      const int id = l1 * L2 + l2;
+      const int* q = leg_charges + (size_t)id * 4 * Dm;
+      if (l2 + 1 < L2) {
+        const int* qn = leg_charges + (size_t)(id + 1) * 4 * Dm;
+        for (int x = 0; x < ctx->dims[id * 4 + 3]; ++x)
+          if (q[3 * Dm + x] != -qn[2 * Dm + x]) return fail(ctx, TNSP_E_ARG, "R/L bond charges are not opposite");
+      }
+      if (l1 + 1 < L1) {
+        const int* qn = leg_charges + (size_t)(id + L2) * 4 * Dm;
+        for (int x = 0; x < ctx->dims[id * 4 + 1]; ++x)
+          if (q[Dm + x] != -qn[x]) return fail(ctx, TNSP_E_ARG, "D/U bond charges are not opposite");
+      }
+    }
+  CK(cudaMemcpy(ctx->d_qleg, leg_charges, sizeof(int) * (size_t)L1 * L2 * 4 * Dm, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_qphys, phys_charges, sizeof(int) * P, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_sflux, site_flux, sizeof(int) * (size_t)L1 * L2, cudaMemcpyHostToDevice));
+  ctx->charged = true;
   return TNSP_OK;
 }
 
@@ -528,10 +630,10 @@ int tnsp_sweep(tnsp_ctx* ctx, int nsweeps, int observe) {
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
   if (nsweeps > 0) {
     if (ctx->precision == TNSP_FP64)
-      sweep_kernel<double><<<grid, kThreads, 0, ctx->stream>>>(md, ch, ctx->slots, (double*)ctx->d_scratch,
+      sweep_kernel<double><<<grid, kThreads, ctx->smem_bytes, ctx->stream>>>(md, ch, ctx->slots, (double*)ctx->d_scratch,
                                                                (const double*)ctx->d_ones, nsweeps, observe, 0);
     else
-      sweep_kernel<float><<<grid, kThreads, 0, ctx->stream>>>(md, ch, ctx->slots, (float*)ctx->d_scratch,
+      sweep_kernel<float><<<grid, kThreads, ctx->smem_bytes, ctx->stream>>>(md, ch, ctx->slots, (float*)ctx->d_scratch,
                                                               (const float*)ctx->d_ones, nsweeps, observe, 0);
     CK(cudaGetLastError());
   }
@@ -632,11 +734,11 @@ int tnsp_amplitude(tnsp_ctx* ctx, int B, const int32_t* configs, double* mantiss
   Model md = make_model(ctx);
   const int grid = std::min(ctx->nslots, B);
   if (ctx->precision == TNSP_FP64)
-    amplitude_kernel<double><<<grid, kThreads, 0, ctx->stream>>>(md, ctx->slots, (double*)ctx->d_scratch,
+    amplitude_kernel<double><<<grid, kThreads, ctx->smem_bytes, ctx->stream>>>(md, ctx->slots, (double*)ctx->d_scratch,
                                                                  (const double*)ctx->d_ones, B, dconf, dm, de,
                                                                  ctx->d_status);
   else
-    amplitude_kernel<float><<<grid, kThreads, 0, ctx->stream>>>(md, ctx->slots, (float*)ctx->d_scratch,
+    amplitude_kernel<float><<<grid, kThreads, ctx->smem_bytes, ctx->stream>>>(md, ctx->slots, (float*)ctx->d_scratch,
                                                                 (const float*)ctx->d_ones, B, dconf, dm, de,
                                                                 ctx->d_status);
   CK(cudaGetLastError());

@@ -55,6 +55,12 @@ class Sampler:
         self._check(
             self.lib.tnsp_lattice_upload(self.ctx, lat.L1, lat.L2, lat.P, ptr(dims, ctypes.c_int),
                                          ptr(flat, ctypes.c_double), self.cut), "tnsp_lattice_upload")
+        ch = lat.charge_arrays()
+        if ch is not None:
+            q, qp, fl = ch
+            self._check(
+                self.lib.tnsp_lattice_charges(self.ctx, ptr(q, ctypes.c_int), ptr(qp, ctypes.c_int),
+                                              ptr(fl, ctypes.c_int)), "tnsp_lattice_charges")
         n, sites, offs, cnts, outs, vals = lat.term_arrays()
         self._check(
             self.lib.tnsp_model_upload(self.ctx, n, ptr(sites, ctypes.c_int), ptr(offs, ctypes.c_int),

@@ -83,6 +83,32 @@ def site_from_blocks(storage, names, edges):
     return np.ascontiguousarray(arr.reshape(shape))
 
 
+def expand_charges(segments):
+    """Per-index charges of an edge given as [(charge, dim), ...]."""
+    return [q for q, d in segments for _ in range(d)]
+
+
+def site_charges(names, edges):
+    """Charges of a reference site tensor: ({"U": [...], "D": [...], "L": [...], "R": [...]},
+    physical charges, flux).  Absent legs get [0]; the one-dimensional total-charge leg T moves to
+    the flux (every block of the reference satisfies sum of charges == 0, T included)."""
+    names = list(names)
+    legs = {}
+    flux = 0
+    phys = None
+    for n, e in zip(names, edges):
+        q = expand_charges(e)
+        if n == "P0":
+            phys = q
+        elif n in ("U", "D", "L", "R"):
+            legs[n] = q
+        else:
+            flux -= sum(q)  # a single index
+    for n in ("U", "D", "L", "R"):
+        legs.setdefault(n, [0])
+    return legs, phys, flux
+
+
 def physics_index(phys_segments, charge, index):
     """``Edge.index_by_point((charge, index))`` on the physical edge."""
     offs, _ = _segment_offsets(phys_segments)
@@ -127,10 +153,14 @@ class SamplingLattice:
     get/set of site tensors, ``_hamiltonians`` (ordered), ``apply_gradient`` and ``lattice_dot``.
     """
 
-    def __init__(self, L1, L2, P, tensors, hamiltonians):
+    def __init__(self, L1, L2, P, tensors, hamiltonians, charges=None):
+        """``charges``: optional (legs, phys, flux) with legs[l1][l2] = {"U": [...], "D": [...],
+        "L": [...], "R": [...]} per-index charges, phys the physical charges and flux[l1][l2] the
+        conserved sum of every nonzero element; enables per-sector factorisation on the device."""
         self.L1 = L1
         self.L2 = L2
         self.P = P
+        self.charges = charges
         self._tensors = [[np.ascontiguousarray(tensors[l1][l2], dtype=np.float64) for l2 in range(L2)]
                          for l1 in range(L1)]
         self._hamiltonians = dict(hamiltonians)  # positions -> element table, reference dict order
@@ -176,6 +206,20 @@ class SamplingLattice:
     def dims(self):
         return np.array([[t.shape[1], t.shape[2], t.shape[3], t.shape[4]] for row in self._tensors for t in row],
                         dtype=np.int32)
+
+    def charge_arrays(self):
+        """(leg_charges, phys_charges, site_flux) in the layout of tnsp_lattice_charges, or None."""
+        if self.charges is None:
+            return None
+        legs, phys, flux = self.charges
+        Dmax = int(self.dims().max())
+        q = np.zeros((self.L1, self.L2, 4, Dmax), dtype=np.int32)
+        for l1, l2 in self.sites():
+            for k, n in enumerate(("U", "D", "L", "R")):
+                v = legs[l1][l2][n]
+                q[l1, l2, k, :len(v)] = v
+        return (np.ascontiguousarray(q.reshape(-1)), np.ascontiguousarray(np.asarray(phys, dtype=np.int32)),
+                np.ascontiguousarray(np.asarray(flux, dtype=np.int32).reshape(-1)))
 
     def flat_tensors(self):
         return np.concatenate([t.reshape(-1) for row in self._tensors for t in row])
@@ -280,6 +324,7 @@ def random_heisenberg(L1, L2, D, seed, scale=True, sectors=None, J=1.0):
     """
     rng = np.random.default_rng(seed)
     tensors = []
+    legs_q = []
     if sectors is None:
         Dv = D
         bond_q = None
@@ -288,6 +333,7 @@ def random_heisenberg(L1, L2, D, seed, scale=True, sectors=None, J=1.0):
         Dv = len(bond_q)
     for l1 in range(L1):
         row = []
+        qrow = []
         for l2 in range(L2):
             U = Dv if l1 > 0 else 1
             Dd = Dv if l1 < L1 - 1 else 1
@@ -302,11 +348,17 @@ def random_heisenberg(L1, L2, D, seed, scale=True, sectors=None, J=1.0):
 
                 mask = u1_allowed_mask([1, -1], qs(U, -1), qs(Dd, 1), qs(L, -1), qs(R, 1))
                 t = t * mask
+                qrow.append({"U": [int(x) for x in qs(U, -1)], "D": [int(x) for x in qs(Dd, 1)],
+                             "L": [int(x) for x in qs(L, -1)], "R": [int(x) for x in qs(R, 1)]})
             if scale:
                 t = t / np.sqrt(2.0 * Dv**z)
             row.append(t)
         tensors.append(row)
-    return SamplingLattice(L1, L2, 2, tensors, nearest_neighbour_terms(L1, L2, heisenberg_table(J)))
+        legs_q.append(qrow)
+    charges = None
+    if bond_q is not None:
+        charges = (legs_q, [1, -1], [[0] * L2 for _ in range(L1)])
+    return SamplingLattice(L1, L2, 2, tensors, nearest_neighbour_terms(L1, L2, heisenberg_table(J)), charges)
 
 
 def neel(L1, L2):
