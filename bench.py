@@ -227,6 +227,8 @@ def run_ours(args):
     h2d = n_params * 8 + n_params * 4 + lat.L1 * lat.L2 * 4 * 4 + int(sum(len(v) for v in lat.term_arrays()[1:]) * 4)
     d2h = 8 * 8 + 2 * n_params * 8 + 3 * B * 8 + 4
     avg_launch_ms = kernel_ms / args.steps
+    cycles = flops[4:]
+    flops = flops[:4]
     achieved = float(flops.sum()) / args.steps / (avg_launch_ms * 1e-3) / 1e9
     if rank != 0:
         return
@@ -274,7 +276,10 @@ def run_ours(args):
                      "flops_per_launch": float(flops.sum()) / args.steps,
                      "flops_split": {"contract": flops[0] / args.steps, "qr": flops[1] / args.steps,
                                      "svd": flops[2] / args.steps, "strip": flops[3] / args.steps},
-                     "traffic": None},
+                     "traffic": None,
+                     "phase_cycle_share": {n: float(c / max(1.0, cycles.sum())) for n, c in
+                                           zip(("two_line", "sectors", "qr", "r_absorb", "jacobi", "svd_out",
+                                                "us_absorb", "strip", "-", "observe", "-", "-"), cycles) if c > 0}},
         "cpu_baseline": cpu,
         "clocks": clocks.summary(),
     }

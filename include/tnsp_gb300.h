@@ -137,10 +137,12 @@ int tnsp_device_status(tnsp_ctx* ctx, int32_t* status);
 int tnsp_last_timing(tnsp_ctx* ctx, double* ms, int64_t* launches);
 
 /*
- * Algorithmic work done by tnsp_sweep since the last reset, in floating-point operations:
- * flops[0] block contractions (2mnk per product), flops[1] Householder QR (with explicit Q),
- * flops[2] truncated SVD (Golub-Van Loan count 4m^2n + 8mn^2 + 9n^3), flops[3] strip
- * environments and holes.  `reset` non-zero zeroes the counters after reading.
+ * Algorithmic work done by tnsp_sweep since the last reset (flops must hold 16 doubles), summed
+ * over blocks: flops[0] block contractions (2mnk per product), flops[1] Householder QR (with
+ * explicit Q), flops[2] truncated SVD (Golub-Van Loan count 4m^2n + 8mn^2 + 9n^3), flops[3] strip
+ * environments and holes; flops[4..15] SM clock cycles spent by the blocks in the phases two-line
+ * contraction, sector analysis, QR, R absorption, Jacobi, SVD output, U*S absorption, strip steps,
+ * (reserved), observation holes, (reserved), (reserved).  `reset` non-zero zeroes the counters.
  * No reference counterpart: instrumentation for the roofline of the sampler kernel.
  */
 int tnsp_counters_read(tnsp_ctx* ctx, double* flops, int reset);

@@ -6,14 +6,13 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libtnsp_gb300.so")
-SOURCES = [os.path.join(CSRC, "tnsp_capi.cu")]
-DEPS = SOURCES + [os.path.join(CSRC, f) for f in ("sampler.cu", "cta_linalg.cuh", "noalloc.cu")] + [
+SOURCES = [os.path.join(CSRC, f) for f in ("sampler_f64.cu", "sampler_f32.cu", "tnsp_capi.cu", "noalloc.cu")]
+DEPS = SOURCES + [os.path.join(CSRC, f) for f in ("sampler_kernels.cuh", "cta_linalg.cuh", "launch.h",
+                                                  "capi_internal.h")] + [
     os.path.join(os.path.dirname(HERE), "include", "tnsp_gb300.h")
 ]
-NVCC_FLAGS = [
-    "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-    "-shared", "-cudart", "shared"
-]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
 
 
 def nvcc():
@@ -31,10 +30,24 @@ def up_to_date():
 
 
 def build(force=False, verbose=False):
-    """Compiles libtnsp_gb300.so next to this file unless it is newer than its sources."""
+    """Compiles libtnsp_gb300.so next to this file unless it is newer than its sources.  The four
+    translation units compile in parallel, then link into one shared library."""
     if not force and up_to_date():
         return OUT
-    cmd = [nvcc()] + NVCC_FLAGS + ["-o", OUT + ".tmp"] + SOURCES
+    objdir = os.path.join(os.path.dirname(HERE), "_build")
+    os.makedirs(objdir, exist_ok=True)
+    procs = []
+    objs = []
+    for src in SOURCES:
+        obj = os.path.join(objdir, os.path.basename(src) + ".o")
+        objs.append(obj)
+        cmd = [nvcc()] + NVCC_FLAGS + ["-c", src, "-o", obj]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        procs.append(subprocess.Popen(cmd))
+    if any(p.wait() != 0 for p in procs):
+        raise RuntimeError("nvcc failed")
+    cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "shared", "-o", OUT + ".tmp"] + objs
     if verbose:
         print(" ".join(cmd), file=sys.stderr)
     subprocess.run(cmd, check=True)

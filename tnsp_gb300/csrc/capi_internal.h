@@ -1,0 +1,117 @@
+// Host-side context of the C ABI and the per-slot scratch plan, shared by tnsp_capi.cu and noalloc.cu.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "../../include/tnsp_gb300.h"
+#include "launch.h"
+
+struct tnsp_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // lattice
+  bool has_lattice = false, has_model = false;
+  int L1 = 0, L2 = 0, P = 0, cut = 0, Dmax = 0;
+  std::vector<int> dims;
+  std::vector<long long> off;
+  long long n_params = 0;
+  double* dA64 = nullptr;
+  float* dA32 = nullptr;
+  int* d_dims = nullptr;
+  long long* d_off = nullptr;
+  std::vector<double> hostA;       // host copy of the site tensors (charge validation)
+  int* d_qleg = nullptr;           // [site][4][Dmax]
+  int* d_qphys = nullptr;          // [P]
+  int* d_sflux = nullptr;          // [site]
+  bool charged = false;
+  // model
+  int n_terms = 0;
+  int* d_term_sites = nullptr;
+  int* d_hterm = nullptr;
+  int* d_vterm = nullptr;
+  int* d_hflip = nullptr;
+  int* d_tab_off = nullptr;
+  int* d_tab_cnt = nullptr;
+  int* d_tab_out = nullptr;
+  double* d_tab_val = nullptr;
+  // chains
+  int B = 0, precision = TNSP_FP64;
+  int32_t* d_conf = nullptr;
+  uint64_t* d_mt = nullptr;
+  int32_t* d_mti = nullptr;
+  double* d_ws_m = nullptr;
+  int32_t* d_ws_e = nullptr;
+  int64_t* d_accepted = nullptr;
+  double* d_acc = nullptr;
+  int32_t* d_status = nullptr;
+  double* d_rec = nullptr;  // 3 x rec_cap x B
+  int rec_cap = 0, rec_n = 0;
+  // slots
+  int nslots = 0;
+  tnsp::Slots slots{};
+  size_t elem = 8;
+  void* d_scratch = nullptr;
+  void* d_ones = nullptr;
+  int* d_ldims = nullptr;
+  int* d_lexp = nullptr;
+  int* d_order = nullptr;
+  double* d_delta = nullptr;
+  double* d_edelta = nullptr;
+  double* d_contrib = nullptr;
+  double* d_red = nullptr;
+  double* d_flops = nullptr;
+  int* d_lq = nullptr;
+  int* d_lfl = nullptr;
+  int* d_tq = nullptr;
+  int* d_tfl = nullptr;
+  int* d_ilist = nullptr;
+  size_t smem_bytes = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0;
+  long long last_launches = 0;
+};
+
+
+namespace tnsp {
+
+// scratch layout of one slot (elements of the sampler's element type)
+inline void plan_slots(const tnsp_ctx* c, Slots& s) {
+  const long long cut = c->cut, D = c->Dmax, Lmax = std::max(c->L1, c->L2);
+  const long long chi = cut * D;
+  s.capB = cut * D * cut;
+  s.capT = chi * D * chi;
+  s.capR = chi * chi;
+  s.capE = cut * D * cut;
+  s.capS = D * D * D * cut * cut;
+  s.capH = D * D * D * D;
+  long long o = 0;
+  auto take = [&](long long n) {
+    const long long r = o;
+    o += (n + 31) / 32 * 32;
+    return r;
+  };
+  s.o_lines[F_UP] = take((long long)c->L1 * c->L2 * s.capB);
+  s.o_lines[F_DOWN] = take((long long)c->L1 * c->L2 * s.capB);
+  s.o_lines[F_LEFT] = take((long long)c->L2 * c->L1 * s.capB);
+  s.o_lines[F_RIGHT] = take((long long)c->L2 * c->L1 * s.capB);
+  s.o_T = take((Lmax + 2) * s.capT);
+  s.o_R = take(s.capR);
+  s.o_tau = take(chi);
+  s.o_X = take(chi * chi);
+  s.o_V = take(chi * chi);
+  s.o_sig = take(chi);
+  s.o_E = take((Lmax + 1) * s.capE);
+  s.o_F = take((Lmax + 1) * s.capE);
+  s.o_t1 = take(s.capS);
+  s.o_t2 = take(s.capS);
+  s.o_w0 = take(s.capE);
+  s.o_w1 = take(s.capE);
+  s.o_h = take(s.capH);
+  s.stride = o;
+}
+
+}  // namespace tnsp

@@ -24,7 +24,10 @@
 // stream capture begins.
 #include <cuda_runtime.h>
 
+#include <cstdio>
 #include <mutex>
+
+#include "capi_internal.h"
 
 namespace tnsp_noalloc {
 
@@ -171,8 +174,7 @@ extern "C" int tnsp_amplitude_noalloc(int L1, int L2, int P, const int* dims, co
   md.qleg = d_qleg;
   md.qphys = d_qphys;
   md.sflux = d_sflux;
-  amplitude_kernel<double><<<nslots, kThreads, 0, st>>>(md, s, d_scratch, d_ones, B, configs, mantissa, exponent,
-                                                        d_status);
+  launch_amplitude_f64(nslots, 0, st, md, s, d_scratch, d_ones, B, configs, mantissa, exponent, d_status);
   if ((e = cudaGetLastError()) != cudaSuccess) return err(TNSP_E_CUDA, "kernel launch failed");
   int32_t status = 0;
   if ((e = cudaMemcpyAsync(&status, d_status, sizeof(int32_t), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||

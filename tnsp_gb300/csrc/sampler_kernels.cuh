@@ -1,4 +1,5 @@
-// Sweep sampling, local energy and gradient holes of a PEPS on one GPU.
+// Sweep sampling, local energy and gradient holes of a PEPS on one GPU (kernel templates; the
+// float64 and float32 instantiations live in sampler_f64.cu and sampler_f32.cu).
 //
 // One thread block owns one Markov chain at a time (persistent blocks stride over thousands of
 // chains).  Inside a block the chain's boundary MPSs, strip environments and compression
@@ -14,6 +15,7 @@
 //  * SweepSampling._single_term / __call__ (tetragono/tetragono/sampling_lattice/sampling.py:117-154)
 //  * Observer.__call__ (tetragono/tetragono/sampling_lattice/observer.py:313-415)
 //  * TAT.random: std::mt19937_64 with libstdc++'s uniform_int / uniform_real (PyTAT/PyTAT.hpp:86-113)
+#pragma once
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -28,6 +30,9 @@ constexpr int kMtN = 312;
 constexpr int kMaxSweepsJacobi = 60;
 constexpr int kMaxSec = 96;     // charge sectors per factorised matrix
 constexpr int kMaxChi = 1024;   // cut * Dmax
+constexpr int kCounters = 16;   // per-slot counters: 4 flop classes + 12 phase cycle counters
+enum { PH_TWOLINE = 0, PH_SECTORS, PH_QR, PH_RABSORB, PH_JACOBI, PH_SVDOUT, PH_USABSORB, PH_STRIP, PH_HOLE,
+       PH_OBSERVE, PH_NORMALIZE, PH_OTHER };
 
 enum { ST_SVD_NOCONV = 1, ST_NONFINITE = 2, ST_UNSUPPORTED = 4, ST_ZERO_WS = 8 };
 enum { F_UP = 0, F_DOWN = 1, F_LEFT = 2, F_RIGHT = 3 };
@@ -92,7 +97,7 @@ struct Slots {
 // ------------------------------------------------------------------------------------------
 // random numbers: std::mt19937_64 + libstdc++ 13 distributions (thread 0 only)
 // ------------------------------------------------------------------------------------------
-__device__ uint64_t mt_next(uint64_t* mt, int& mti) {
+__device__ inline uint64_t mt_next(uint64_t* mt, int& mti) {
   if (mti >= kMtN) {
     for (int i = 0; i < kMtN; ++i) {
       const uint64_t x = (mt[i] & 0xFFFFFFFF80000000ull) | (mt[(i + 1) % kMtN] & 0x7FFFFFFFull);
@@ -112,7 +117,7 @@ __device__ uint64_t mt_next(uint64_t* mt, int& mti) {
 
 // std::uniform_int_distribution<int>(0, n-1): Lemire's nearly-divisionless downscaling on a
 // 128-bit product (bits/uniform_int_dist.h, _S_nd).
-__device__ int draw_uniform_int(uint64_t* mt, int& mti, int n) {
+__device__ inline int draw_uniform_int(uint64_t* mt, int& mti, int n) {
   const uint64_t range = (uint64_t)n;
   uint64_t x = mt_next(mt, mti);
   uint64_t lo = x * range;
@@ -130,7 +135,7 @@ __device__ int draw_uniform_int(uint64_t* mt, int& mti, int n) {
 
 // std::uniform_real_distribution<double>(0, 1): generate_canonical<double, 53> with one 64-bit
 // word: round-to-nearest conversion, division by 2^64, clamp to below 1.
-__device__ double draw_uniform_real(uint64_t* mt, int& mti) {
+__device__ inline double draw_uniform_real(uint64_t* mt, int& mti) {
   const uint64_t x = mt_next(mt, mti);
   double r = __ull2double_rn(x) * 5.421010862427522e-20;  // 2^-64, exact
   if (r >= 1.0) r = 0.99999999999999989;
@@ -167,10 +172,15 @@ template <class T> struct Chain {
   int* eF;
   T* red;
   double* dred;
-  double* fl;             // shared [4] flop counters (thread 0 adds)
+  double* fl;             // shared [kCounters]: flop counters [0..3], phase cycles [4..]
 
   __device__ void count(int k, double f) const {
     if (threadIdx.x == 0) fl[k] += f;
+  }
+  // phase timer: thread 0 reads the SM clock at phase boundaries (already barrier points)
+  __device__ long long tic() const { return clock64(); }
+  __device__ void toc(int phase, long long t0) const {
+    if (threadIdx.x == 0) fl[4 + phase] += (double)(clock64() - t0);
   }
 
   __device__ T* line(int f, int idx, int i) const {
@@ -404,6 +414,8 @@ template <class T> struct Engine : Chain<T> {
   using Chain<T>::site;
   using Chain<T>::lexp;
   using Chain<T>::order;
+  using Chain<T>::tic;
+  using Chain<T>::toc;
   const T* ones;
   int32_t* status;
   int* lq;
@@ -519,6 +531,7 @@ template <class T> struct Engine : Chain<T> {
     if (threadIdx.x < n + 2) s_buf[threadIdx.x] = threadIdx.x;
     __syncthreads();
     int expo = lexpo(f, prev);
+    long long t0 = tic();
     for (int i = 0; i < n; ++i) {
       const int l1 = (f < 2) ? idx : i, l2 = (f < 2) ? i : idx;
       const SiteView w = site(l1, l2, conf[l1 * md.L2 + l2], orient);
@@ -541,6 +554,7 @@ template <class T> struct Engine : Chain<T> {
       }
       __syncthreads();
     }
+    toc(PH_TWOLINE, t0);
     T* Rb = slot + sl.o_R;
     T* tau = slot + sl.o_tau;
     T* sm = smem;
@@ -553,7 +567,10 @@ template <class T> struct Engine : Chain<T> {
       const int* qL = tqL(i);
       const int* qD = tqD(i);
       const int* qR = tqR(i);
+      t0 = tic();
       sectors(rows, cols, [&](int x) { return qL[x / d] + qD[x % d]; }, [&](int z) { return qR[z]; }, F, &s_sec, s_sh);
+      toc(PH_SECTORS, t0);
+      t0 = tic();
       const int ns = s_sec.n;
       int ktot = 0;
       for (int t = 0; t < ns; ++t) ktot += min(s_sec.m[t], s_sec.c[t]);
@@ -607,6 +624,8 @@ template <class T> struct Engine : Chain<T> {
         koff += kr;
         rsz += (double)kr * mc;
       }
+      toc(PH_QR, t0);
+      t0 = tic();
       // new T[i+1] (ktot x d'B') = R * T[i+1], sector by sector, into G
       const int dB = s_dd[i + 1] * s_dB[i + 1];
       {
@@ -647,6 +666,7 @@ template <class T> struct Engine : Chain<T> {
       }
       __syncthreads();
       expo += block_normalize(Tbuf(s_buf[i + 1]), (long long)ktot * dB, red);
+      toc(PH_RABSORB, t0);
     }
     // ---------------- truncating SVD sweep, per sector, global cut ----------------
     T* X = slot + sl.o_X;
@@ -657,8 +677,11 @@ template <class T> struct Engine : Chain<T> {
       const int* qL = tqL(i);
       const int* qD = tqD(i);
       const int* qR = tqR(i);
+      t0 = tic();
       sectors(rows, cols, [&](int x) { return qL[x]; }, [&](int z) { return qD[z / Bc] + qR[z % Bc]; }, F, &s_sec,
               s_sh);
+      toc(PH_SECTORS, t0);
+      t0 = tic();
       const int ns = s_sec.n;
       if (threadIdx.x == 0) {
         int xo = 0, vo = 0, so = 0;
@@ -709,6 +732,8 @@ template <class T> struct Engine : Chain<T> {
         }
         __syncthreads();
       }
+      toc(PH_JACOBI, t0);
+      t0 = tic();
       const int c = md.cut < S ? md.cut : S;
       // global selection: descending value, ties to the earlier sector / lower index
       for (int j = threadIdx.x; j < S; j += blockDim.x) {
@@ -760,6 +785,8 @@ template <class T> struct Engine : Chain<T> {
         }
       }
       __syncthreads();
+      toc(PH_SVDOUT, t0);
+      t0 = tic();
       // new T[i-1] (A d x c) = T[i-1] * US, summing only over the rows of each kept vector's sector
       {
         const int Ad = s_dA[i - 1] * s_dd[i - 1];
@@ -799,6 +826,7 @@ template <class T> struct Engine : Chain<T> {
       }
       __syncthreads();
       expo += block_normalize(Tbuf(s_buf[i - 1]), (long long)s_dA[i - 1] * s_dd[i - 1] * c, red);
+      toc(PH_USABSORB, t0);
     }
     if (n == 1) expo += block_normalize(Tbuf(s_buf[0]), (long long)s_dA[0] * s_dd[0] * s_dB[0], red);
     // store the line with its charges
@@ -888,6 +916,7 @@ template <class T> struct Engine : Chain<T> {
 
   // E[c+1] = E[c] x column c (physical index s); writes into dst with exponent returned
   __device__ int step_left(int kind, int idx, int c, const T* Ein, Dims3 e, int s, T* dst) {
+    const long long t0 = tic();
     int l1, l2;
     strip_site_rc(kind, idx, c, l1, l2);
     const SiteView w = site(l1, l2, s, kind == 0 ? 0 : 2);
@@ -896,9 +925,12 @@ template <class T> struct Engine : Chain<T> {
     const Dims3 up = lsdim(fup(kind), idx - 1, c), dn = lsdim(fdn(kind), idx + 1, c);
     this->count(3, 2.0 * ((double)e.a * e.p * e.b * up.p * up.b + (double)e.b * up.b * dn.p * w.dr * e.p * up.p +
                           (double)up.b * w.dr * dn.b * e.b * dn.p));
-    return block_normalize(dst, (long long)up.b * w.dr * dn.b, red);
+    const int ex = block_normalize(dst, (long long)up.b * w.dr * dn.b, red);
+    toc(PH_STRIP, t0);
+    return ex;
   }
   __device__ int step_right(int kind, int idx, int c, const T* Fin, Dims3 f, int s, T* dst) {
+    const long long t0 = tic();
     int l1, l2;
     strip_site_rc(kind, idx, c, l1, l2);
     const SiteView w = site(l1, l2, s, kind == 0 ? 0 : 2);
@@ -907,7 +939,9 @@ template <class T> struct Engine : Chain<T> {
     const Dims3 up = lsdim(fup(kind), idx - 1, c), dn = lsdim(fdn(kind), idx + 1, c);
     this->count(3, 2.0 * ((double)up.a * up.p * f.a * f.p * f.b + (double)up.a * w.dl * dn.p * f.b * up.p * f.p +
                           (double)up.a * w.dl * dn.a * dn.p * f.b));
-    return block_normalize(dst, (long long)up.a * w.dl * dn.a, red);
+    const int ex = block_normalize(dst, (long long)up.a * w.dl * dn.a, red);
+    toc(PH_STRIP, t0);
+    return ex;
   }
 
   __device__ int conf_at(int kind, int idx, int c) const {
@@ -1106,8 +1140,8 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Sl
   __shared__ double s_ws_m, s_h0_m;
   __shared__ int s_strip_kind, s_strip_idx, s_strip_eupto, s_strip_ffrom;
   __shared__ int64_t s_accepted;
-  __shared__ double s_fl[4];
-  if (threadIdx.x < 4) s_fl[threadIdx.x] = 0.0;
+  __shared__ double s_fl[kCounters];
+  if (threadIdx.x < kCounters) s_fl[threadIdx.x] = 0.0;
   __syncthreads();
   const int nsite = md.L1 * md.L2;
   Engine<T> eng{{md, sl, scratch + (long long)blockIdx.x * sl.stride, (const T*)md.A,
@@ -1234,6 +1268,7 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Sl
       }
       __syncthreads();
       const double eloc = s_eloc;
+      const long long t_obs = eng.tic();
       if (!zero_ws) {
         // holes: d psi / d A[l1,l2] / ws, accumulated with weight rw and E_loc * rw
         for (int l1 = 0; l1 < md.L1; ++l1) {
@@ -1267,6 +1302,7 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Sl
           }
         }
       }
+      eng.toc(PH_OBSERVE, t_obs);
       if (threadIdx.x == 0) {
         double* acc = ch.acc + (long long)b * 8;
         acc[0] += 1.0;
@@ -1298,7 +1334,7 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Sl
     }
     __syncthreads();
   }
-  if (threadIdx.x < 4) sl.flops[(long long)blockIdx.x * 4 + threadIdx.x] += s_fl[threadIdx.x];
+  if (threadIdx.x < kCounters) sl.flops[(long long)blockIdx.x * kCounters + threadIdx.x] += s_fl[threadIdx.x];
 }
 
 // amplitude hole(()) of arbitrary configurations (no RNG, no accumulators)
@@ -1312,8 +1348,8 @@ __global__ void __launch_bounds__(kThreads) amplitude_kernel(Model md, Slots sl,
   __shared__ T s_red[kWarps];
   __shared__ double s_dred[kWarps];
   __shared__ int s_strip_kind, s_strip_idx, s_strip_eupto, s_strip_ffrom;
-  __shared__ double s_fl[4];
-  if (threadIdx.x < 4) s_fl[threadIdx.x] = 0.0;
+  __shared__ double s_fl[kCounters];
+  if (threadIdx.x < kCounters) s_fl[threadIdx.x] = 0.0;
   __syncthreads();
   const int nsite = md.L1 * md.L2;
   Engine<T> eng{{md, sl, scratch + (long long)blockIdx.x * sl.stride, (const T*)md.A,
@@ -1339,27 +1375,5 @@ __global__ void __launch_bounds__(kThreads) amplitude_kernel(Model md, Slots sl,
     __syncthreads();
   }
 }
-
-// sum the per-slot gradient accumulators in slot order (deterministic)
-__global__ void reduce_slots(const double* __restrict__ src, int nslots, long long n, double* __restrict__ dst) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    double s = 0.0;
-    for (int k = 0; k < nslots; ++k) s += src[(long long)k * n + i];
-    dst[i] = s;
-  }
-}
-
-template <class T> __global__ void fill_ones(T* p) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) p[0] = (T)1;
-}
-
-template __global__ void sweep_kernel<double>(Model, Chains, Slots, double*, const double*, int, int, int);
-template __global__ void sweep_kernel<float>(Model, Chains, Slots, float*, const float*, int, int, int);
-template __global__ void amplitude_kernel<double>(Model, Slots, double*, const double*, int, const int32_t*, double*,
-                                                  int32_t*, int32_t*);
-template __global__ void amplitude_kernel<float>(Model, Slots, float*, const float*, int, const int32_t*, double*,
-                                                 int32_t*, int32_t*);
-template __global__ void fill_ones<double>(double*);
-template __global__ void fill_ones<float>(float*);
 
 }  // namespace tnsp

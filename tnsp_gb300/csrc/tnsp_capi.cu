@@ -1,5 +1,5 @@
-// C ABI of the sampler (declared in include/tnsp_gb300.h).  Host-side plan, buffers and
-// launches; the kernels are in sampler.cu (compiled into this translation unit).
+// C ABI of the sampler (declared in include/tnsp_gb300.h): host-side plan, buffers and launches.
+// The kernels are instantiated in sampler_f64.cu / sampler_f32.cu and reached through launch.h.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -10,75 +10,24 @@
 #include <vector>
 
 #include "../../include/tnsp_gb300.h"
-#include "sampler.cu"
+#include "capi_internal.h"
 
 using namespace tnsp;
 
-struct tnsp_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  std::string err;
-  // lattice
-  bool has_lattice = false, has_model = false;
-  int L1 = 0, L2 = 0, P = 0, cut = 0, Dmax = 0;
-  std::vector<int> dims;
-  std::vector<long long> off;
-  long long n_params = 0;
-  double* dA64 = nullptr;
-  float* dA32 = nullptr;
-  int* d_dims = nullptr;
-  long long* d_off = nullptr;
-  std::vector<double> hostA;       // host copy of the site tensors (charge validation)
-  int* d_qleg = nullptr;           // [site][4][Dmax]
-  int* d_qphys = nullptr;          // [P]
-  int* d_sflux = nullptr;          // [site]
-  bool charged = false;
-  // model
-  int n_terms = 0;
-  int* d_term_sites = nullptr;
-  int* d_hterm = nullptr;
-  int* d_vterm = nullptr;
-  int* d_hflip = nullptr;
-  int* d_tab_off = nullptr;
-  int* d_tab_cnt = nullptr;
-  int* d_tab_out = nullptr;
-  double* d_tab_val = nullptr;
-  // chains
-  int B = 0, precision = TNSP_FP64;
-  int32_t* d_conf = nullptr;
-  uint64_t* d_mt = nullptr;
-  int32_t* d_mti = nullptr;
-  double* d_ws_m = nullptr;
-  int32_t* d_ws_e = nullptr;
-  int64_t* d_accepted = nullptr;
-  double* d_acc = nullptr;
-  int32_t* d_status = nullptr;
-  double* d_rec = nullptr;  // 3 x rec_cap x B
-  int rec_cap = 0, rec_n = 0;
-  // slots
-  int nslots = 0;
-  Slots slots{};
-  size_t elem = 8;
-  void* d_scratch = nullptr;
-  void* d_ones = nullptr;
-  int* d_ldims = nullptr;
-  int* d_lexp = nullptr;
-  int* d_order = nullptr;
-  double* d_delta = nullptr;
-  double* d_edelta = nullptr;
-  double* d_contrib = nullptr;
-  double* d_red = nullptr;
-  double* d_flops = nullptr;
-  int* d_lq = nullptr;
-  int* d_lfl = nullptr;
-  int* d_tq = nullptr;
-  int* d_tfl = nullptr;
-  int* d_ilist = nullptr;
-  size_t smem_bytes = 0;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  double last_ms = 0;
-  long long last_launches = 0;
-};
+namespace tnsp {
+// sum the per-slot gradient accumulators in slot order (deterministic)
+__global__ void reduce_slots(const double* __restrict__ src, int nslots, long long n, double* __restrict__ dst) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int k = 0; k < nslots; ++k) s += src[(long long)k * n + i];
+    dst[i] = s;
+  }
+}
+
+template <class T> __global__ void fill_ones(T* p) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) p[0] = (T)1;
+}
+}  // namespace tnsp
 
 namespace {
 
@@ -200,42 +149,6 @@ Chains make_chains(tnsp_ctx* c) {
   return ch;
 }
 
-// scratch layout of one slot (elements of the sampler's element type)
-void plan_slots(tnsp_ctx* c, Slots& s) {
-  const long long cut = c->cut, D = c->Dmax, Lmax = std::max(c->L1, c->L2);
-  const long long chi = cut * D;
-  s.capB = cut * D * cut;
-  s.capT = chi * D * chi;
-  s.capR = chi * chi;
-  s.capE = cut * D * cut;
-  s.capS = D * D * D * cut * cut;
-  s.capH = D * D * D * D;
-  long long o = 0;
-  auto take = [&](long long n) {
-    const long long r = o;
-    o += (n + 31) / 32 * 32;
-    return r;
-  };
-  s.o_lines[F_UP] = take((long long)c->L1 * c->L2 * s.capB);
-  s.o_lines[F_DOWN] = take((long long)c->L1 * c->L2 * s.capB);
-  s.o_lines[F_LEFT] = take((long long)c->L2 * c->L1 * s.capB);
-  s.o_lines[F_RIGHT] = take((long long)c->L2 * c->L1 * s.capB);
-  s.o_T = take((Lmax + 2) * s.capT);
-  s.o_R = take(s.capR);
-  s.o_tau = take(chi);
-  s.o_X = take(chi * chi);
-  s.o_V = take(chi * chi);
-  s.o_sig = take(chi);
-  s.o_E = take((Lmax + 1) * s.capE);
-  s.o_F = take((Lmax + 1) * s.capE);
-  s.o_t1 = take(s.capS);
-  s.o_t2 = take(s.capS);
-  s.o_w0 = take(s.capE);
-  s.o_w1 = take(s.capE);
-  s.o_h = take(s.capH);
-  s.stride = o;
-}
-
 int ensure_slots(tnsp_ctx* ctx) {
   if (ctx->nslots > 0) return 0;
   int sms = 0;
@@ -259,7 +172,7 @@ int ensure_slots(tnsp_ctx* ctx) {
   CK(cudaMalloc((void**)&ctx->d_edelta, sizeof(double) * ctx->n_params * ctx->nslots));
   CK(cudaMalloc((void**)&ctx->d_contrib, sizeof(double) * std::max(1, ctx->n_terms) * ctx->nslots));
   CK(cudaMalloc((void**)&ctx->d_red, sizeof(double) * ctx->n_params * 2));
-  CK(cudaMalloc((void**)&ctx->d_flops, sizeof(double) * 4 * ctx->nslots));
+  CK(cudaMalloc((void**)&ctx->d_flops, sizeof(double) * kCounters * ctx->nslots));
   {
     const long long chi = (long long)ctx->cut * ctx->Dmax;
     CK(cudaMalloc((void**)&ctx->d_lq, sizeof(int) * 4 * kMaxL * kMaxL * 2 * ctx->cut * ctx->nslots));
@@ -270,14 +183,11 @@ int ensure_slots(tnsp_ctx* ctx) {
   }
   // dynamic shared memory for sector staging: 96 KB keeps two blocks per SM
   ctx->smem_bytes = 96 * 1024;
-  if (ctx->precision == TNSP_FP64) {
-    CK(cudaFuncSetAttribute(sweep_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_bytes));
-    CK(cudaFuncSetAttribute(amplitude_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_bytes));
-  } else {
-    CK(cudaFuncSetAttribute(sweep_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_bytes));
-    CK(cudaFuncSetAttribute(amplitude_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_bytes));
-  }
-  CK(cudaMemsetAsync(ctx->d_flops, 0, sizeof(double) * 4 * ctx->nslots, ctx->stream));
+  if (ctx->precision == TNSP_FP64)
+    CK(set_smem_limit_f64((int)ctx->smem_bytes));
+  else
+    CK(set_smem_limit_f32((int)ctx->smem_bytes));
+  CK(cudaMemsetAsync(ctx->d_flops, 0, sizeof(double) * kCounters * ctx->nslots, ctx->stream));
   CK(cudaMemsetAsync(ctx->d_delta, 0, sizeof(double) * ctx->n_params * ctx->nslots, ctx->stream));
   CK(cudaMemsetAsync(ctx->d_edelta, 0, sizeof(double) * ctx->n_params * ctx->nslots, ctx->stream));
   if (ctx->precision == TNSP_FP64)
@@ -630,11 +540,11 @@ int tnsp_sweep(tnsp_ctx* ctx, int nsweeps, int observe) {
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
   if (nsweeps > 0) {
     if (ctx->precision == TNSP_FP64)
-      sweep_kernel<double><<<grid, kThreads, ctx->smem_bytes, ctx->stream>>>(md, ch, ctx->slots, (double*)ctx->d_scratch,
-                                                               (const double*)ctx->d_ones, nsweeps, observe, 0);
+      launch_sweep_f64(grid, ctx->smem_bytes, ctx->stream, md, ch, ctx->slots, ctx->d_scratch, ctx->d_ones, nsweeps,
+                       observe, 0);
     else
-      sweep_kernel<float><<<grid, kThreads, ctx->smem_bytes, ctx->stream>>>(md, ch, ctx->slots, (float*)ctx->d_scratch,
-                                                              (const float*)ctx->d_ones, nsweeps, observe, 0);
+      launch_sweep_f32(grid, ctx->smem_bytes, ctx->stream, md, ch, ctx->slots, ctx->d_scratch, ctx->d_ones, nsweeps,
+                       observe, 0);
     CK(cudaGetLastError());
   }
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
@@ -734,13 +644,11 @@ int tnsp_amplitude(tnsp_ctx* ctx, int B, const int32_t* configs, double* mantiss
   Model md = make_model(ctx);
   const int grid = std::min(ctx->nslots, B);
   if (ctx->precision == TNSP_FP64)
-    amplitude_kernel<double><<<grid, kThreads, ctx->smem_bytes, ctx->stream>>>(md, ctx->slots, (double*)ctx->d_scratch,
-                                                                 (const double*)ctx->d_ones, B, dconf, dm, de,
-                                                                 ctx->d_status);
+    launch_amplitude_f64(grid, ctx->smem_bytes, ctx->stream, md, ctx->slots, ctx->d_scratch, ctx->d_ones, B, dconf,
+                         dm, de, ctx->d_status);
   else
-    amplitude_kernel<float><<<grid, kThreads, ctx->smem_bytes, ctx->stream>>>(md, ctx->slots, (float*)ctx->d_scratch,
-                                                                (const float*)ctx->d_ones, B, dconf, dm, de,
-                                                                ctx->d_status);
+    launch_amplitude_f32(grid, ctx->smem_bytes, ctx->stream, md, ctx->slots, ctx->d_scratch, ctx->d_ones, B, dconf,
+                         dm, de, ctx->d_status);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(mantissa, dm, sizeof(double) * B, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(exponent, de, sizeof(int32_t) * B, cudaMemcpyDeviceToHost, ctx->stream));
@@ -772,11 +680,11 @@ int tnsp_counters_read(tnsp_ctx* ctx, double* flops, int reset) {
   if (!ctx->nslots) return fail(ctx, TNSP_E_STATE, "no chains");
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
-  std::vector<double> f((size_t)4 * ctx->nslots);
+  std::vector<double> f((size_t)kCounters * ctx->nslots);
   CK(cudaMemcpy(f.data(), ctx->d_flops, sizeof(double) * f.size(), cudaMemcpyDeviceToHost));
-  for (int k = 0; k < 4; ++k) {
+  for (int k = 0; k < kCounters; ++k) {
     double s = 0;
-    for (int i = 0; i < ctx->nslots; ++i) s += f[(size_t)i * 4 + k];
+    for (int i = 0; i < ctx->nslots; ++i) s += f[(size_t)i * kCounters + k];
     flops[k] = s;
   }
   if (reset) CK(cudaMemset(ctx->d_flops, 0, sizeof(double) * f.size()));
@@ -785,4 +693,3 @@ int tnsp_counters_read(tnsp_ctx* ctx, double* flops, int reset) {
 
 }  // extern "C"
 
-#include "noalloc.cu"

@@ -130,9 +130,12 @@ class Sampler:
         self._check(self.lib.tnsp_device_status(self.ctx, ctypes.byref(st)), "tnsp_device_status")
         return st.value
 
+    PHASES = ("two_line", "sectors", "qr", "r_absorb", "jacobi", "svd_out", "us_absorb", "strip", "-", "observe",
+              "-", "-")
+
     def counters(self, reset=True):
-        """Algorithmic flops since the last reset: [contractions, QR, SVD, strips/holes]."""
-        f = np.zeros(4)
+        """[contraction, QR, SVD, strip] flops then 12 phase cycle counters, since the last reset."""
+        f = np.zeros(16)
         self._check(self.lib.tnsp_counters_read(self.ctx, ptr(f, ctypes.c_double), 1 if reset else 0),
                     "tnsp_counters_read")
         return f
