@@ -10,7 +10,7 @@
 
 namespace tnsp {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
 
 template <class T> struct Eps;
@@ -388,5 +388,6 @@ template <class T> __device__ void block_orgqr_cm(int m, int k, T* G, const T* t
     __syncthreads();
   }
 }
+
 
 }  // namespace tnsp

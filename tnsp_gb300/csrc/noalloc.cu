@@ -120,8 +120,8 @@ extern "C" int tnsp_amplitude_noalloc(int L1, int L2, int P, const int* dims, co
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) == cudaSuccess &&
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0 &&
-      nslots > 2 * sms)
-    nslots = 2 * sms;
+      nslots > 4 * sms)
+    nslots = 4 * sms;
   unsigned char* base = nullptr;
   cudaError_t e = arena_for_current_device(&base);
   if (e != cudaSuccess) return err(TNSP_E_CUDA, "cudaGetSymbolAddress failed");

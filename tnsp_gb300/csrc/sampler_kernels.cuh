@@ -1100,8 +1100,10 @@ __device__ void single_term(Engine<T>& eng, const Model& md, int kind, int idx, 
     int mti = *s_mti;
     const double u = draw_uniform_real(mt, mti);
     *s_mti = mti;
+    // IEEE semantics as in the reference: ws == 0 gives p = inf (accepted) or, for 0/0, NaN
+    // (rejected); the event is recorded in the status word, not treated as a failure
     s_acc = u < p;
-    if (!isfinite(p)) atomicOr(eng.status, ST_NONFINITE);
+    if (*s_ws_m == 0.0) atomicOr(eng.status, ST_ZERO_WS);
     s_m = m;
     s_e = ex;
     s_skip = (na == sa && nb == sb);
