@@ -1,0 +1,45 @@
+"""The reference's gradient_descent sampling loop, run unchanged against the drop-in classes."""
+import numpy as np
+import pytest
+
+from golden_cases import Golden
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name", ["heis_no_3x3_D3_dc4", "heis_u1_4x4_D111_dc5"])
+def test_driver_loop_matches_reference(name):
+    from test_gpu_parity import make_lattice
+    from tnsp_gb300.sampling import Observer, SweepSampling
+    g = Golden(name)
+    state = make_lattice(g, charged=True)
+    seeds = g.meta["chain_seeds"]
+    chains = len(seeds)
+    nt, ns = g.meta["n_therm"], g.meta["n_samples"]
+    observer = Observer(state, enable_energy=True, enable_gradient=True)
+    # thermalisation (gm_conf_eq): sweeps without an observer
+    sampling = SweepSampling(state, g.cut, None, None, chains=chains, seeds=seeds)
+    sampling.configuration.import_configuration(g.neel()[:, :, None])
+    for k in range(nt * chains):
+        possibility, configuration = sampling()
+        ci = k % chains
+        np.testing.assert_array_equal(configuration.export_configuration()[:, :, 0], g.z["confs"][ci][k // chains])
+    # gradient.py:331-358
+    with observer:
+        for k in range(ns * chains):
+            possibility, configuration = sampling()
+            observer(possibility, configuration)
+            ci = k % chains
+            assert abs(possibility / g.z["possibility"][ci][nt + k // chains] - 1) < 1e-10
+    energy, error = observer.energy
+    assert abs(energy - g.z["energy"][0]) < 1e-12
+    grad = observer.gradient
+    for l1 in range(g.L1):
+        for l2 in range(g.L2):
+            ref = g.z[f"grad_{l1}_{l2}"]
+            assert np.abs(grad[l1][l2] - ref).max() <= 1e-10 * max(1.0, np.abs(ref).max())
+    # apply_gradient + normalize_lattice as gradient.py:399-433 does
+    norm0 = state.lattice_dot()
+    state.apply_gradient(grad, 0.01)
+    observer.normalize_lattice()
+    assert state.lattice_dot() != norm0

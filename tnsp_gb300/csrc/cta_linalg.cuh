@@ -390,4 +390,128 @@ template <class T> __device__ void block_orgqr_cm(int m, int k, T* G, const T* t
 }
 
 
+
+// ---------------------------------------------------------------------------------------------
+// one-sided Jacobi on several independent vector sets at once
+// ---------------------------------------------------------------------------------------------
+// Set t has nv[t] vectors of length len[t] at Xs[t] (vector-major) and accumulates its rotations
+// into Vs[t] (nv[t] x nv[t], set to the identity here); each set may live in shared or global memory.  Every set follows its own
+// circle ordering and convergence test (rotation rule and tolerance of block_jacobi, noise floor
+// tol^2 * |A|_F^2), but all sets advance together: a block barrier ends one round of every set, so
+// the number of barriers is set by the largest set instead of the sum over sets.  Pairs of a round
+// are spread over the warps.  Returns the largest sweep count, or -1 if a set hit max_sweeps.
+template <class T, int MAXS>
+__device__ int block_jacobi_multi(int ns, const int* nv, const int* len, T* const* Xs, T* const* Vs, int max_sweeps) {
+  __shared__ int s_np[MAXS], s_pp[MAXS + 1], s_rot[MAXS], s_done[MAXS], s_sweeps[MAXS];
+  __shared__ T s_noise[MAXS];
+  __shared__ int s_active, s_fail;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int t = 0; t < ns; ++t)
+    for (long e = threadIdx.x; e < (long)nv[t] * nv[t]; e += blockDim.x)
+      Vs[t][e] = (e / nv[t] == e % nv[t]) ? (T)1 : (T)0;
+  // squared Frobenius norm of each set (invariant under the rotations, >= sigma_max^2): the noise
+  // floor below which a vector is left alone is tol^2 * |A|_F^2
+  if (threadIdx.x < MAXS) s_noise[threadIdx.x] = 0;
+  __syncthreads();
+  for (int t = 0; t < ns; ++t) {
+    T acc = 0;
+    for (long e = threadIdx.x; e < (long)nv[t] * len[t]; e += blockDim.x) acc = fma(Xs[t][e], Xs[t][e], acc);
+    acc = warp_sum(acc);
+    if (lane == 0) atomicAdd(&s_noise[t], acc);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int pp = 0;
+    for (int t = 0; t < ns; ++t) {
+      const T tol = Eps<T>::value() * (T)len[t];
+      s_noise[t] = s_noise[t] * tol * tol;
+      s_np[t] = nv[t] + (nv[t] & 1);
+      s_pp[t] = pp;
+      pp += nv[t] >= 2 ? s_np[t] / 2 : 0;
+      s_rot[t] = 0;
+      s_done[t] = nv[t] < 2;
+      s_sweeps[t] = 0;
+    }
+    s_pp[ns] = pp;
+    s_fail = 0;
+  }
+  __syncthreads();
+  for (int g = 0;; ++g) {
+    // pairs of round g of every unfinished set
+    const int total = s_pp[ns];
+    for (int p = w; p < total; p += kWarps) {
+      int t = 0;
+      while (p >= s_pp[t + 1]) ++t;
+      if (s_done[t]) continue;
+      const int np = s_np[t], k = p - s_pp[t], rounds = np - 1;
+      const int round = g % rounds;
+      const int i = k == 0 ? 0 : ((k + round - 1) % rounds) + 1;
+      const int j = ((np - 1 - k + round - 1) % rounds) + 1;
+      if (i >= nv[t] || j >= nv[t]) continue;
+      const int L = len[t];
+      T* xi = Xs[t] + (long)i * L;
+      T* xj = Xs[t] + (long)j * L;
+      T a = 0, b = 0, c2 = 0;
+      for (int r = lane; r < L; r += 32) {
+        const T u = xi[r], v = xj[r];
+        a = fma(u, u, a);
+        b = fma(v, v, b);
+        c2 = fma(u, v, c2);
+      }
+      a = warp_sum(a);
+      b = warp_sum(b);
+      c2 = warp_sum(c2);
+      const T tol = Eps<T>::value() * (T)L;
+      if (a <= s_noise[t] || b <= s_noise[t]) continue;
+      if (!(fabs(c2) > tol * sqrt(a) * sqrt(b))) continue;
+      if (lane == 0) s_rot[t] = 1;
+      const T zeta = (b - a) / ((T)2 * c2);
+      const T tt = (zeta >= 0 ? (T)1 : (T)-1) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
+      const T c = (T)1 / sqrt((T)1 + tt * tt);
+      const T sn = c * tt;
+      for (int r = lane; r < L; r += 32) {
+        const T u = xi[r], v = xj[r];
+        xi[r] = c * u - sn * v;
+        xj[r] = sn * u + c * v;
+      }
+      const int n = nv[t];
+      T* vi = Vs[t] + (long)i * n;
+      T* vj = Vs[t] + (long)j * n;
+      for (int r = lane; r < n; r += 32) {
+        const T u = vi[r], v = vj[r];
+        vi[r] = c * u - sn * v;
+        vj[r] = sn * u + c * v;
+      }
+    }
+    __syncthreads();
+    // end of a sweep of some sets: converged or next sweep
+    if (threadIdx.x == 0) {
+      int active = 0;
+      for (int t = 0; t < ns; ++t) {
+        if (s_done[t]) continue;
+        const int rounds = s_np[t] - 1;
+        if ((g + 1) % rounds == 0) {
+          ++s_sweeps[t];
+          if (!s_rot[t]) {
+            s_done[t] = 1;
+          } else if (s_sweeps[t] >= max_sweeps) {
+            s_done[t] = 1;
+            s_fail = 1;
+          }
+          s_rot[t] = 0;
+        }
+        active += !s_done[t];
+      }
+      s_active = active;
+    }
+    __syncthreads();
+    if (s_active == 0) break;
+  }
+  int mx = 0;
+  for (int t = 0; t < ns; ++t) mx = max(mx, s_sweeps[t]);
+  const int fail = s_fail;
+  __syncthreads();
+  return fail ? -1 : mx;
+}
+
 }  // namespace tnsp

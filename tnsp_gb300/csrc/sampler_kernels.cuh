@@ -626,18 +626,45 @@ template <class T> struct Engine : Chain<T> {
       }
       toc(PH_QR, t0);
       t0 = tic();
-      // new T[i+1] (ktot x d'B') = R * T[i+1], sector by sector, into G
+      // new T[i+1] (ktot x d'B') = R * T[i+1], sector by sector, into G; each thread owns a 4x4
+      // output tile (4 rows of one sector's R x 4 columns), so one load of T feeds 4 FMAs
       const int dB = s_dd[i + 1] * s_dB[i + 1];
       {
         const T* Tn = Tbuf(s_buf[i + 1]);
-        for (long long e = threadIdx.x; e < (long long)ktot * dB; e += blockDim.x) {
-          const int k = (int)(e / dB), col = (int)(e % dB);
-          const int t = s_kmap[k], y = s_kloc[k], mc = s_sec.c[t];
-          const T* rr = Rb + s_roffs[t] + (long long)y * mc;
+        const int tc = (dB + 3) / 4;
+        int kof = 0;
+        for (int t = 0; t < ns; ++t) {
+          const int mc = s_sec.c[t], kr = min(s_sec.m[t], mc);
+          const T* rb = Rb + s_roffs[t];
           const int* C_ = cl + s_sec.co[t];
-          T acc = 0;
-          for (int z = y; z < mc; ++z) acc = fma(rr[z], Tn[(long long)C_[z] * dB + col], acc);
-          G[e] = acc;
+          const int tr = (kr + 3) / 4;
+          for (long long tile = threadIdx.x; tile < (long long)tr * tc; tile += blockDim.x) {
+            const int y0 = (int)(tile / tc) * 4, c0 = (int)(tile % tc) * 4;
+            T acc[4][4];
+#pragma unroll
+            for (int v = 0; v < 4; ++v)
+#pragma unroll
+              for (int u = 0; u < 4; ++u) acc[v][u] = (T)0;
+            for (int z = y0; z < mc; ++z) {
+              const T* trow = Tn + (long long)C_[z] * dB + c0;
+              T tv[4];
+#pragma unroll
+              for (int u = 0; u < 4; ++u) tv[u] = (c0 + u < dB) ? trow[u] : (T)0;
+#pragma unroll
+              for (int v = 0; v < 4; ++v) {
+                const T rv = (y0 + v < kr) ? rb[(long long)(y0 + v) * mc + z] : (T)0;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) acc[v][u] = fma(rv, tv[u], acc[v][u]);
+              }
+            }
+#pragma unroll
+            for (int v = 0; v < 4; ++v)
+              if (y0 + v < kr)
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                  if (c0 + u < dB) G[(long long)(kof + y0 + v) * dB + c0 + u] = acc[v][u];
+          }
+          kof += kr;
         }
         this->count(0, 2.0 * dB * rsz);
       }
@@ -699,39 +726,67 @@ template <class T> struct Engine : Chain<T> {
       int S = 0;
       for (int t = 0; t < ns; ++t) S += min(s_sec.m[t], s_sec.c[t]);
       const T* M = Tbuf(s_buf[i]);
+      // gather every sector's vectors (columns when the block is tall, rows when wide); sectors are
+      // staged in shared memory while it has room, the others work in the slot's X/V arrays
+      __shared__ int s_nvv[kMaxSec], s_lenv[kMaxSec];
+      __shared__ T* s_xp[kMaxSec];
+      __shared__ T* s_vp[kMaxSec];
+      if (threadIdx.x == 0) {
+        long long used = 0;
+        for (int t = 0; t < ns; ++t) {
+          const int nv = min(s_sec.m[t], s_sec.c[t]), len = max(s_sec.m[t], s_sec.c[t]);
+          s_nvv[t] = nv;
+          s_lenv[t] = len;
+          const long long need = (long long)nv * len + (long long)nv * nv;
+          if (used + need <= smcap) {
+            s_xp[t] = sm + used;
+            s_vp[t] = sm + used + (long long)nv * len;
+            used += need;
+          } else {
+            s_xp[t] = X + s_xo[t];
+            s_vp[t] = V + s_vo[t];
+          }
+        }
+      }
+      __syncthreads();
       for (int t = 0; t < ns; ++t) {
         const int mr = s_sec.m[t], mc = s_sec.c[t];
         const bool caseA = mc <= mr;
         const int nv = caseA ? mc : mr, len = caseA ? mr : mc;
         const int* R_ = rl + s_sec.ro[t];
         const int* C_ = cl + s_sec.co[t];
-        const bool in_smem = (long long)nv * len + (long long)nv * nv <= smcap;
-        T* x = in_smem ? sm : X + s_xo[t];
-        T* v = in_smem ? sm + (long long)nv * len : V + s_vo[t];
+        T* x = s_xp[t];
         for (long long e = threadIdx.x; e < (long long)nv * len; e += blockDim.x) {
           const int j = (int)(e / len), q = (int)(e % len);
           x[e] = caseA ? M[(long long)R_[q] * cols + C_[j]] : M[(long long)R_[j] * cols + C_[q]];
         }
-        __syncthreads();
-        const int sweeps = block_jacobi(nv, len, x, v, kMaxSweepsJacobi);
-        if (sweeps < 0 && threadIdx.x == 0) atomicOr(status, ST_SVD_NOCONV);
-        {
-          const double mm = len, nn = nv;
-          this->count(2, 4.0 * mm * mm * nn + 8.0 * mm * nn * nn + 9.0 * nn * nn * nn);
-        }
-        const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-        for (int j = wp; j < nv; j += kWarps) {
-          T s2 = 0;
-          for (int q = lane; q < len; q += 32) s2 = fma(x[(long long)j * len + q], x[(long long)j * len + q], s2);
-          s2 = warp_sum(s2);
-          if (lane == 0) sig[s_so[t] + j] = sqrt(s2);
-        }
-        if (in_smem) {
-          for (long long e = threadIdx.x; e < (long long)nv * len; e += blockDim.x) X[s_xo[t] + e] = x[e];
-          for (long long e = threadIdx.x; e < (long long)nv * nv; e += blockDim.x) V[s_vo[t] + e] = v[e];
-        }
-        __syncthreads();
+        const double mm = len, nn = nv;
+        this->count(2, 4.0 * mm * mm * nn + 8.0 * mm * nn * nn + 9.0 * nn * nn * nn);
       }
+      __syncthreads();
+      const int sweeps = block_jacobi_multi<T, kMaxSec>(ns, s_nvv, s_lenv, s_xp, s_vp, kMaxSweepsJacobi);
+      if (sweeps < 0 && threadIdx.x == 0) atomicOr(status, ST_SVD_NOCONV);
+      {
+        const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+        for (int t = 0; t < ns; ++t) {
+          const int nv = s_nvv[t], len = s_lenv[t];
+          const T* x = s_xp[t];
+          for (int j = wp; j < nv; j += kWarps) {
+            T s2 = 0;
+            for (int q = lane; q < len; q += 32) s2 = fma(x[(long long)j * len + q], x[(long long)j * len + q], s2);
+            s2 = warp_sum(s2);
+            if (lane == 0) sig[s_so[t] + j] = sqrt(s2);
+          }
+        }
+      }
+      // results of shared-memory sectors back to the packed X/V arrays read by the output stage
+      for (int t = 0; t < ns; ++t) {
+        if (s_xp[t] == X + s_xo[t]) continue;
+        const int nv = s_nvv[t], len = s_lenv[t];
+        for (long long e = threadIdx.x; e < (long long)nv * len; e += blockDim.x) X[s_xo[t] + e] = s_xp[t][e];
+        for (long long e = threadIdx.x; e < (long long)nv * nv; e += blockDim.x) V[s_vo[t] + e] = s_vp[t][e];
+      }
+      __syncthreads();
       toc(PH_JACOBI, t0);
       t0 = tic();
       const int c = md.cut < S ? md.cut : S;

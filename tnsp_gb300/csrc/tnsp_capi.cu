@@ -156,8 +156,8 @@ int ensure_slots(tnsp_ctx* ctx) {
   Slots s{};
   plan_slots(ctx, s);
   ctx->elem = ctx->precision == TNSP_FP64 ? 8 : 4;
-  // as many resident blocks as fit: 4 per SM, bounded by a scratch budget of 64 GB
-  long long want = 4LL * sms;
+  // as many resident blocks as fit: 3 per SM, bounded by a scratch budget of 64 GB
+  long long want = 3LL * sms;
   const long long per = s.stride * (long long)ctx->elem + 2LL * ctx->n_params * 8;
   const long long budget = 64LL << 30;
   want = std::min(want, std::max(1LL, budget / std::max(1LL, per)));
@@ -181,8 +181,9 @@ int ensure_slots(tnsp_ctx* ctx) {
     CK(cudaMalloc((void**)&ctx->d_tfl, sizeof(int) * kMaxL * ctx->nslots));
     CK(cudaMalloc((void**)&ctx->d_ilist, sizeof(int) * (chi * ctx->Dmax + chi) * ctx->nslots));
   }
-  // dynamic shared memory for sector staging: 44 KB keeps four blocks per SM
-  ctx->smem_bytes = 44 * 1024;
+  // dynamic shared memory for sector staging: 64 KB keeps three blocks per SM (the register
+  // budget of the sweep kernel allows three 128-thread blocks)
+  ctx->smem_bytes = 64 * 1024;
   if (ctx->precision == TNSP_FP64)
     CK(set_smem_limit_f64((int)ctx->smem_bytes));
   else

@@ -236,9 +236,14 @@ class SamplingLattice:
         return out
 
     def apply_gradient(self, gradient, step_size):
-        """``SamplingLattice.apply_gradient`` (lattice.py:936-948) for real tensors."""
+        """``SamplingLattice.apply_gradient`` (lattice.py:936-948) for real tensors; ``gradient`` is
+        indexed [l1][l2] (or [l1, l2] for a numpy object array)."""
         for l1, l2 in self.sites():
-            self[l1, l2] = self._tensors[l1][l2] - step_size * gradient[l1][l2]
+            g = gradient[l1, l2] if isinstance(gradient, np.ndarray) else gradient[l1][l2]
+            self[l1, l2] = self._tensors[l1][l2] - step_size * g
+
+    def bcast_lattice(self, root=0):
+        """One process owns every chain: nothing to broadcast (lattice.py:950-954)."""
 
     def lattice_dot(self, a=None, b=None):
         a = self._tensors if a is None else a

@@ -1,0 +1,209 @@
+"""Drop-in mirrors of tetragono's ``SweepSampling``, ``Configuration`` and ``Observer``.
+
+The reference runs one Markov chain per process and calls, once per sample
+(tetragono/tetragono/sampling_lattice/gradient.py:331-358)::
+
+    with seed_differ, observer:
+        sampling = SweepSampling(state, cut, restrict, hopping)
+        sampling.configuration.import_configuration(configs)
+        for step in range(total):
+            possibility, configuration = sampling()
+            observer(possibility, configuration)
+
+The same loop runs unchanged here.  ``SweepSampling`` owns ``chains`` Markov chains on the GPU;
+its first call sweeps all of them in one launch (observing every new configuration in the same
+kernel when an ``Observer`` is entered on the lattice) and the following calls hand out the other
+chains' samples without device work.  ``Observer.__call__`` therefore only checks the pairing: the
+accumulation already happened on the device, and ``energy`` / ``gradient`` read the reduced
+accumulators.
+
+Only the features of the sweep / E_loc / gradient path are mirrored: no restricted subspace other
+than charge conservation, no custom hopping Hamiltonians, no extra observer sets, no natural
+gradient, no configuration cache (``NotImplementedError`` where the reference would accept them).
+"""
+import numpy as np
+
+from .engine import Sampler, estimators, gradient_from
+from ._lib import TNSP_FP32, TNSP_FP64
+
+
+class Configuration:
+    """One chain's configuration (``Configuration``, tetragono/tetragono/sampling_lattice/lattice.py:27-416),
+    as seen by the driver: indexing and export/import of the int64 [L1, L2, orbit] array."""
+
+    def __init__(self, owner, config):
+        self.owner = owner
+        self._config = np.array(config, dtype=np.int64).reshape(owner.L1, owner.L2)
+
+    def __getitem__(self, l1l2o):
+        l1, l2, orbit = l1l2o
+        if orbit != 0:
+            raise KeyError(l1l2o)
+        return int(self._config[l1, l2])
+
+    def export_configuration(self):
+        return self._config[:, :, None].copy()
+
+    def valid(self):
+        return True
+
+
+class _PendingImport(Configuration):
+    """``SweepSampling.configuration`` before the first sweep: importing sets every chain."""
+
+    def __init__(self, sampling):
+        super().__init__(sampling.owner, np.zeros((sampling.owner.L1, sampling.owner.L2), dtype=np.int64))
+        self._sampling = sampling
+
+    def import_configuration(self, config):
+        config = np.asarray(config, dtype=np.int64)
+        if config.ndim == 3:
+            config = config[:, :, 0]
+        if config.shape != (self.owner.L1, self.owner.L2):
+            raise ValueError("configuration shape mismatch")
+        self._config = config.copy()
+        self._sampling._set_start(config)
+
+
+class SweepSampling:
+    """``SweepSampling(owner, cut_dimension, restrict_subspace, hopping_hamiltonians)``
+    (tetragono/tetragono/sampling_lattice/sampling.py:74-193) over ``chains`` GPU chains.
+
+    ``seeds`` (one per chain) seed each chain's mt19937_64 as ``TAT.random.seed`` would; by default
+    chain b uses seed ``seed_base + b``.  ``discard`` skips that many uniform_real draws first (the
+    driver's ``SeedDiffer`` discards one)."""
+
+    def __init__(self, owner, cut_dimension, restrict_subspace=None, hopping_hamiltonians=None, *, chains=1,
+                 seeds=None, seed_base=0, discard=0, precision="fp64", device=0):
+        if restrict_subspace is not None:
+            raise NotImplementedError("restrict_subspace: only charge conservation of the model is supported")
+        if hopping_hamiltonians is not None:
+            raise NotImplementedError("custom hopping Hamiltonians are not supported")
+        self.owner = owner
+        self._cut_dimension = cut_dimension
+        self.chains = chains
+        self.seeds = np.asarray(seeds if seeds is not None else np.arange(chains) + seed_base, dtype=np.uint64)
+        if self.seeds.shape != (chains,):
+            raise ValueError("one seed per chain")
+        self.discard = discard
+        self.precision = TNSP_FP32 if precision == "fp32" else TNSP_FP64
+        self._engine = Sampler(owner, cut_dimension, device=device)
+        owner._gpu_engine = self._engine
+        self._started = False
+        self._buffer = []
+        self.configuration = _PendingImport(self)
+
+    def _set_start(self, config):
+        self._engine.init_chains(np.asarray(config, dtype=np.int32), self.seeds, discard=self.discard,
+                                 precision=self.precision)
+        self._started = True
+
+    def refresh_all(self):
+        """The lattice tensors changed: upload them (chains keep their configurations)."""
+        self._engine.upload()
+
+    def __call__(self):
+        if not self._started:
+            raise RuntimeError("Configuration not initialized")
+        if not self._buffer:
+            observer = getattr(self.owner, "_active_observer", None)
+            observing = observer is not None
+            if observing and observer._engine is not self._engine:
+                observer._bind(self._engine)
+            if self._engine._uploaded_version != self.owner.version:
+                self._engine.upload()
+            self._engine.sweep(1, observe=observing)
+            conf, logp = self._engine.read_chains()
+            self._buffer = [(float(np.exp(lp)), Configuration(self.owner, c), observing) for c, lp in zip(conf, logp)]
+            self._buffer.reverse()
+        possibility, configuration, observed = self._buffer.pop()
+        configuration._observed = observed
+        self.configuration = configuration
+        return possibility, configuration
+
+
+class Observer:
+    """``Observer`` (tetragono/tetragono/sampling_lattice/observer.py:28-920) for energy and gradient."""
+
+    def __init__(self, owner, *, observer_set=None, enable_energy=False, enable_gradient=False,
+                 enable_natural_gradient=False, cache_natural_delta=None, cache_configuration=False,
+                 restrict_subspace=None, classical_energy=None):
+        if observer_set or enable_natural_gradient or cache_natural_delta or cache_configuration or \
+                restrict_subspace is not None or classical_energy is not None:
+            raise NotImplementedError("only energy and gradient observation are supported")
+        self.owner = owner
+        self._enable_energy = enable_energy or enable_gradient
+        self._enable_gradient = enable_gradient
+        self._engine = None
+        self._count = 0
+        self._scalars = None
+        self._delta = None
+        self._edelta = None
+
+    def __enter__(self):
+        """``Observer.__enter__``: the accumulators start empty; they are bound to the sampler whose
+        first sweep happens inside this context (the driver creates the SweepSampling after entering)."""
+        self._engine = None
+        self._count = 0
+        self._scalars = None
+        self.owner._active_observer = self
+        return self
+
+    def _bind(self, engine):
+        if self._engine is not None:
+            raise RuntimeError("one observer context observes one SweepSampling")
+        self._engine = engine
+        engine.reset_observer()
+
+    def __exit__(self, exc_type, exc_val, exc_tb):
+        self.owner._active_observer = None
+        if exc_type is not None:
+            return False
+        if self._engine is not None:
+            self._scalars, self._delta, self._edelta = self._engine.read_observer(
+                with_gradient=self._enable_gradient)
+        return False
+
+    def __call__(self, possibility, configuration):
+        if not getattr(configuration, "_observed", False):
+            raise RuntimeError("the configuration was sampled outside this observer's context")
+        self._count += 1
+
+    def _read(self):
+        if self._scalars is None:
+            self._scalars, self._delta, self._edelta = self._engine.read_observer(with_gradient=self._enable_gradient)
+        return self._scalars
+
+    @property
+    def total_energy(self):
+        e, d = estimators(self._read(), 1)
+        return e, d
+
+    @property
+    def energy(self):
+        return estimators(self._read(), self.owner.site_number)
+
+    @property
+    def gradient(self):
+        """2 conj(<E Delta> - <E><Delta>) per site tensor, dense (P, U, D, L, R) arrays."""
+        if not self._enable_gradient:
+            raise RuntimeError("gradient not enabled")
+        scal = self._read()
+        return self.owner.unflatten(gradient_from(scal, self._delta, self._edelta))
+
+    @property
+    def instability(self):
+        s = self._read()
+        N, R, RR = s[0], s[1], s[2]
+        expect = R / N
+        var = RR / N - expect**2
+        return (var**0.5 if var > 0 else 0.0) / expect
+
+    def normalize_lattice(self):
+        """``Observer.normalize_lattice`` (observer.py:909-920): rescale every site tensor by
+        exp(mean log|ws| / site_number)."""
+        s = self._read()
+        mean_log_ws = s[3] / s[0]
+        param = np.exp(mean_log_ws / self.owner.site_number)
+        for l1, l2 in self.owner.sites():
+            self.owner[l1, l2] = self.owner[l1, l2] / param
