@@ -6,10 +6,15 @@ Effective samples/s = samples/s / (2 tau_int(E_loc)), tau_int estimated from the
 series (pooled autocorrelation, Sokal window c=5).
 
 Workloads (seeded synthetic PEPS, no dataset involved):
-  heis4x4  4x4 Heisenberg (J=1), no symmetry, D=4, Dcut=16, tensors N(0,1)/sqrt(2 D^z),
-           Neel start, 64 thermalisation sweeps, 1024 chains (1024 samples per step)
+  heis4x4    4x4 Heisenberg (J=1), no symmetry, D=4, Dcut=16, tensors N(0,1)/sqrt(2 D^z),
+             Neel start, 64 thermalisation sweeps, 1024 chains (1024 samples per step)
   heis8x8u1  8x8 Heisenberg, U(1) bonds {-1:2, 0:2, +1:2} (D=6), Dcut=36, blocks N(0,1),
-           Neel start (total Sz = 0), 4096 chains
+             Neel start (total Sz = 0), 456 chains = one resident wave of 3 blocks x 152 SMs
+             (the 4096-sample launch runs the same kernel for nine waves), 2 thermalisation sweeps
+             (throughput does not depend on thermalisation)
+
+With --precision fp32 the chains' final configurations are re-evaluated in float64 (observe-only
+launch) and the E_loc and energy-per-site differences are reported under "fp64_check".
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--precision fp64|fp32]
 python bench.py --impl reference ...   (the oracle restatement of the reference on host cores)
@@ -29,9 +34,9 @@ sys.path.insert(0, ROOT)
 
 WORKLOADS = {
     "heis4x4": dict(L1=4, L2=4, D=4, sectors=None, cut=16, scale=True, chains=1024, therm=64),
-    "heis8x8u1": dict(L1=8, L2=8, D=6, sectors=(2, 2, 2), cut=36, scale=False, chains=4096, therm=16),
+    "heis8x8u1": dict(L1=8, L2=8, D=6, sectors=(2, 2, 2), cut=36, scale=False, chains=456, therm=2),
 }
-DEFAULT_WORKLOAD = "heis4x4"
+DEFAULT_WORKLOAD = "heis8x8u1"
 FP64_NOMINAL_GFLOPS = 1250.0
 
 
@@ -70,14 +75,14 @@ def _cpu_worker(args):
     w = WORKLOADS[workload]
     lat = make_lattice(w)
     peps = DensePEPS([[lat[l1, l2] for l2 in range(lat.L2)] for l1 in range(lat.L1)], list(lat._hamiltonians.items()),
-                     w["cut"])
+                     w["cut"], lat.charges)
     chain = SweepChain(peps, neel(lat.L1, lat.L2), seed)
     acc = ObserverAccumulator(peps)
     t0 = time.perf_counter()
     elocs = []
     while time.perf_counter() - t0 < seconds and len(elocs) < max_samples:
         poss, conf = chain.sweep()
-        _, e, _ = acc.add(poss, conf)
+        _, e, _ = acc.add(poss, conf, chain.env)
         elocs.append(e)
     return len(elocs), time.perf_counter() - t0, elocs
 
@@ -202,6 +207,19 @@ def run_ours(args):
         t_dev = float(tt.item())
         dist.barrier()
     flops = s.counters(reset=True)
+    fp64_check = None
+    if prec == TNSP_FP32:
+        # the same configurations observed in float64: E_loc and energy-per-site error of float32
+        conf, _ = s.read_chains()
+        e32 = np.asarray(elocs[-1])
+        s64 = Sampler(lat, w["cut"], device=local)
+        s64.init_chains(conf, seeds, precision=TNSP_FP64)
+        s64.sweep(0, observe=True)
+        e64 = s64.read_samples(1)[0][0]
+        s64.close()
+        fp64_check = {"chains": int(B), "eloc_max_abs_err": float(np.abs(e32 - e64).max()),
+                      "eloc_max_rel_err": float((np.abs(e32 - e64) / np.maximum(np.abs(e64), 1e-300)).max()),
+                      "energy_per_site_err": float(abs(e32.mean() - e64.mean()) / lat.site_number)}
     # end-to-end through the public C ABI with host buffers: upload the tensors, sweep + observe,
     # read the accumulators (energy scalars, Delta, E*Delta) and the per-sample record
     n_params = int(sum(lat[l1, l2].size for l1, l2 in lat.sites()))
@@ -282,6 +300,7 @@ def run_ours(args):
                                                 "us_absorb", "strip", "-", "observe", "-", "-"), cycles) if c > 0}},
         "cpu_baseline": cpu,
         "clocks": clocks.summary(),
+        "fp64_check": fp64_check,
     }
     print(json.dumps(out))
 

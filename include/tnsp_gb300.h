@@ -96,6 +96,8 @@ int tnsp_chains_init(tnsp_ctx* ctx, int B, const int32_t* configs, const uint64_
  * Runs `nsweeps` sweeps of every chain.  When `observe` is non-zero every sweep is followed by
  * the observation of its configuration: E_loc, the gradient holes and the reweighted
  * accumulators (energy, Delta, E*Delta), and per-sample E_loc and log|ws| are recorded.
+ * nsweeps == 0 with observe != 0 observes the chains' current configurations once (sampling
+ * weight |ws|^2 of the configuration itself), e.g. to re-evaluate configurations in another precision.
  * Replaces: SweepSampling.__call__ (sampling.py:145-154, with _single_term :117-143) and
  * Observer.__call__ (tetragono/tetragono/sampling_lattice/observer.py:313-415).
  */

@@ -29,6 +29,12 @@ What is restated, with the reference lines it follows:
   (tetragono/tetragono/sampling_lattice/sampling.py:117-190);
 * ``Observer.__call__`` and the estimators (tetragono/tetragono/sampling_lattice/observer.py:313-415,
   433-469, 528-555).
+
+With charges (Bose U(1)) every QR and SVD of the compression is done per charge sector, with the
+truncation keeping the largest singular values over all sectors, as TAT's block-sparse qr / svd
+do (TAT/include/TAT/implement/qr.hpp:310-510, svd.hpp:259-532); the boundaries are cached and
+invalidated like the reference's lazy DAG (only the lines containing a changed site are dropped),
+so the oracle's cost per sample follows the reference's.
 """
 
 import numpy as np
@@ -44,36 +50,97 @@ def ones_line(n):
     return [np.ones((1, 1, 1)) for _ in range(n)]
 
 
-def compress(line, sites, cut):
+def ones_charges(n):
+    return [(np.zeros(1, int), np.zeros(1, int), 0) for _ in range(n)]
+
+
+def _sectors(qrow, qcol, F):
+    """[(r, rows, cols)] for the block structure qrow + qcol == F, row charges ascending."""
+    out = []
+    for r in sorted(set(qrow.tolist())):
+        rows = np.nonzero(qrow == r)[0]
+        cols = np.nonzero(qcol == F - r)[0]
+        if len(rows) and len(cols):
+            out.append((r, rows, cols))
+    return out
+
+
+def compress(line, sites, cut, line_q=None, site_q=None):
     """``_two_line_to_one_line`` on dense tensors.
 
     ``line[i]`` has shape (a, p, b): left bond, open leg towards ``sites``, right bond.
     ``sites[i]`` has shape (u, d, l, r) with ``u`` contracted against ``line``'s ``p``.
-    Returns the new line, tensors (a', d, b').
+    ``line_q[i]`` = (qa, qb, flux) and ``site_q[i]`` = (qu, qd, ql, qr, flux) are index charges
+    (None: no symmetry).  Returns the new line, tensors (a', d, b'), and its charges.
     """
     n = len(line)
-    T = []
+    T, qA, qD, qB, F = [], [], [], [], []
     for i in range(n):
         a, p, b = line[i].shape
         u, d, l, r = sites[i].shape
         assert p == u
-        t = np.einsum("apb,pdlr->aldbr", line[i], sites[i]).reshape(a * l, d, b * r)
-        T.append(t)
-    # QR sweep (single_layer_auxiliaries.py:484-488)
+        t = np.tensordot(line[i], sites[i], axes=([1], [0]))  # (a, b, d, l, r)
+        T.append(t.transpose(0, 3, 2, 1, 4).reshape(a * l, d, b * r))
+        la, lb, lf = line_q[i] if line_q is not None else (np.zeros(a, int), np.zeros(b, int), 0)
+        _, sd, sl, sr, sf = site_q[i] if site_q is not None else (None, np.zeros(d, int), np.zeros(l, int),
+                                                                    np.zeros(r, int), 0)
+        qA.append((np.asarray(la)[:, None] + np.asarray(sl)[None, :]).reshape(-1))
+        qD.append(np.asarray(sd))
+        qB.append((np.asarray(lb)[:, None] + np.asarray(sr)[None, :]).reshape(-1))
+        F.append(lf + sf)
+    # QR sweep, per sector (single_layer_auxiliaries.py:484-488)
     for i in range(n - 1):
-        a, d, b = T[i].shape
-        q, r = np.linalg.qr(T[i].reshape(a * d, b))
-        k = q.shape[1]
-        T[i] = q.reshape(a, d, k)
-        T[i + 1] = np.einsum("kb,bdc->kdc", r, T[i + 1])
-    # SVD sweep with truncation (single_layer_auxiliaries.py:490-496)
+        A, d, B = T[i].shape
+        M = T[i].reshape(A * d, B)
+        qrow = (qA[i][:, None] + qD[i][None, :]).reshape(-1)
+        secs = _sectors(qrow, qB[i], F[i])
+        ktot = sum(min(len(rows), len(cols)) for _, rows, cols in secs)
+        Q = np.zeros((A * d, ktot))
+        R = np.zeros((ktot, B))
+        qk = np.zeros(ktot, int)
+        k0 = 0
+        for r, rows, cols in secs:
+            q, rr = np.linalg.qr(M[np.ix_(rows, cols)])
+            k = q.shape[1]
+            Q[rows, k0:k0 + k] = q
+            R[k0:k0 + k][:, cols] = rr
+            qk[k0:k0 + k] = r
+            k0 += k
+        T[i] = Q.reshape(A, d, ktot)
+        b_, d_, c_ = T[i + 1].shape
+        T[i + 1] = (R @ T[i + 1].reshape(b_, d_ * c_)).reshape(ktot, d_, c_)
+        qB[i] = -qk
+        qA[i + 1] = qk
+        F[i + 1] += F[i]
+        F[i] = 0
+    # SVD sweep with truncation over all sectors (single_layer_auxiliaries.py:490-496, svd.hpp:429-470)
     for i in reversed(range(1, n)):
-        a, d, b = T[i].shape
-        U, S, Vh = np.linalg.svd(T[i].reshape(a, d * b), full_matrices=False)
-        c = min(cut, S.shape[0])
-        T[i] = Vh[:c].reshape(c, d, b)
-        T[i - 1] = np.einsum("adb,bc->adc", T[i - 1], U[:, :c] * S[None, :c])
-    return T
+        A, d, B = T[i].shape
+        M = T[i].reshape(A, d * B)
+        qcol = (qD[i][:, None] + qB[i][None, :]).reshape(-1)
+        secs = _sectors(qA[i], qcol, F[i])
+        found = []
+        for si, (r, rows, cols) in enumerate(secs):
+            U, S, Vh = np.linalg.svd(M[np.ix_(rows, cols)], full_matrices=False)
+            for j in range(len(S)):
+                found.append((-S[j], si, j, U[:, j] * S[j], Vh[j]))
+        found.sort(key=lambda x: (x[0], x[1], x[2]))
+        kept = found[:min(cut, len(found))]
+        c = len(kept)
+        Vnew = np.zeros((c, d * B))
+        US = np.zeros((A, c))
+        qk = np.zeros(c, int)
+        for t, (_, si, _, us, vh) in enumerate(kept):
+            r, rows, cols = secs[si]
+            Vnew[t, cols] = vh
+            US[rows, t] = us
+            qk[t] = r
+        T[i] = Vnew.reshape(c, d, B)
+        a_, d_, b_ = T[i - 1].shape
+        T[i - 1] = (T[i - 1].reshape(a_ * d_, b_) @ US).reshape(a_, d_, c)
+        qA[i] = qk
+        qB[i - 1] = -qk
+    return T, [(qA[i], qB[i], F[i]) for i in range(n)]
 
 
 # ----------------------------------------------------------------------------------------------
@@ -81,12 +148,16 @@ def compress(line, sites, cut):
 # ----------------------------------------------------------------------------------------------
 def strip_step_left(E, up, site, down):
     """E (x, y, z) -> E' (a, r, b): absorb one column of a three-line strip from the left."""
-    return np.einsum("xyz,xua,udyr,zdb->arb", E, up, site, down, optimize=True)
+    t1 = np.tensordot(E, up, axes=([0], [0]))  # (y, z, u, a)
+    t2 = np.tensordot(t1, site, axes=([0, 2], [2, 0]))  # (z, a, d, r)
+    return np.tensordot(t2, down, axes=([0, 2], [0, 1]))  # (a, r, b)
 
 
 def strip_step_right(F, up, site, down):
     """F (a, r, b) -> F' (x, l, z): absorb one column of a three-line strip from the right."""
-    return np.einsum("arb,xua,udlr,zdb->xlz", F, up, site, down, optimize=True)
+    s1 = np.tensordot(up, F, axes=([2], [0]))  # (x, u, r, b)
+    s2 = np.tensordot(s1, site, axes=([1, 2], [0, 3]))  # (x, b, d, l)
+    return np.tensordot(s2, down, axes=([1, 2], [2, 1])).transpose(0, 1, 2)  # (x, l, z)
 
 
 def strip_envs(up, sites, down):
@@ -111,7 +182,10 @@ def strip_value(up, sites, down):
 
 def strip_hole(E_left, up, down, F_right):
     """d value / d site, shape (u, d, l, r)."""
-    return np.einsum("xlz,xua,zdb,arb->udlr", E_left, up, down, F_right, optimize=True)
+    h1 = np.tensordot(E_left, up, axes=([0], [0]))  # (l, z, u, a)
+    h2 = np.tensordot(h1, down, axes=([1], [0]))  # (l, u, a, d, b)
+    h = np.tensordot(h2, F_right, axes=([2, 4], [0, 2]))  # (l, u, d, r)
+    return h.transpose(1, 2, 0, 3)
 
 
 # ----------------------------------------------------------------------------------------------
@@ -126,13 +200,26 @@ class DensePEPS:
     (tetragono/tetragono/tensor_element.py:91-108).  Only orbit 0 is supported.
     """
 
-    def __init__(self, tensors, terms, cut):
+    def __init__(self, tensors, terms, cut, charges=None):
+        """``charges``: optional (legs, phys, flux) as in tnsp_gb300.lattice.SamplingLattice."""
         self.A = tensors
         self.L1 = len(tensors)
         self.L2 = len(tensors[0])
         self.terms = terms
         self.cut = cut
         self.site_number = self.L1 * self.L2
+        self.charges = charges
+
+    def site_q(self, l1, l2, s, orient):
+        """Index charges (qu, qd, ql, qr, flux) of the projected site in one of the orientations
+        used by row_sites / col_sites: 0 row, 1 row flipped, 2 column, 3 column flipped."""
+        if self.charges is None:
+            return None
+        legs, phys, flux = self.charges
+        q = {k: np.asarray(v, int) for k, v in legs[l1][l2].items()}
+        f = flux[l1][l2] - phys[s]
+        U, D, L, R = q["U"], q["D"], q["L"], q["R"]
+        return [(U, D, L, R, f), (D, U, L, R, f), (L, R, U, D, f), (R, L, U, D, f)][orient]
 
     # projected sites in the four orientations -------------------------------------------
     def site(self, l1, l2, s):
@@ -146,6 +233,11 @@ class DensePEPS:
             out.append(t.transpose(1, 0, 2, 3) if flip else t)
         return out
 
+    def row_q(self, conf, l1, flip=False):
+        if self.charges is None:
+            return None
+        return [self.site_q(l1, l2, conf[l1, l2], 1 if flip else 0) for l2 in range(self.L2)]
+
     def col_sites(self, conf, l2, flip=False):
         """Column l2 as a "row": (l, r, u, d) orientation; ``flip`` -> (r, l, u, d)."""
         out = []
@@ -154,13 +246,21 @@ class DensePEPS:
             out.append(t.transpose(3, 2, 0, 1) if flip else t.transpose(2, 3, 0, 1))
         return out
 
+    def col_q(self, conf, l2, flip=False):
+        if self.charges is None:
+            return None
+        return [self.site_q(l1, l2, conf[l1, l2], 3 if flip else 2) for l1 in range(self.L1)]
+
 
 class Environment:
-    """All boundaries and strips of one configuration (what the lazy DAG would hold)."""
+    """All boundaries and strips of one configuration (what the lazy DAG would hold).
+
+    ``update`` changes sites and drops exactly the cached boundaries that contain them, as an
+    accepted hop resets the reference's lazy nodes (lazy_graph/lazy/__init__.py ``Node.reset``)."""
 
     def __init__(self, peps, conf):
         self.peps = peps
-        self.conf = conf
+        self.conf = np.array(conf)
         self._up = {}
         self._down = {}
         self._left = {}
@@ -168,40 +268,62 @@ class Environment:
         self._row_envs = {}
         self._col_envs = {}
 
+    def update(self, changes):
+        for l1, l2, s in changes:
+            self.conf[l1, l2] = s
+            for k in [k for k in self._up if k >= l1]:
+                del self._up[k]
+            for k in [k for k in self._down if k <= l1]:
+                del self._down[k]
+            for k in [k for k in self._left if k >= l2]:
+                del self._left[k]
+            for k in [k for k in self._right if k <= l2]:
+                del self._right[k]
+        self._row_envs = {}
+        self._col_envs = {}
+
+    def _line(self, cache, k, edge, n, prev, sites, sq):
+        if k == edge:
+            return ones_line(n), ones_charges(n)
+        if k not in cache:
+            line, lq = prev()
+            cache[k] = compress(line, sites(), self.peps.cut, lq if self.peps.charges is not None else None, sq())
+        return cache[k]
+
     # boundary families (single_layer_auxiliaries.py:430-456) ------------------------------
-    def up(self, l1):
+    def up_q(self, l1):
         """``_up_to_down[l1]``: rows 0..l1 compressed from the top; open legs point down."""
         p = self.peps
-        if l1 == -1:
-            return ones_line(p.L2)
-        if l1 not in self._up:
-            self._up[l1] = compress(self.up(l1 - 1), p.row_sites(self.conf, l1), p.cut)
-        return self._up[l1]
+        return self._line(self._up, l1, -1, p.L2, lambda: self.up_q(l1 - 1), lambda: p.row_sites(self.conf, l1),
+                          lambda: p.row_q(self.conf, l1))
 
-    def down(self, l1):
+    def down_q(self, l1):
         """``_down_to_up[l1]``: rows l1..L1-1 compressed from the bottom; open legs point up."""
         p = self.peps
-        if l1 == p.L1:
-            return ones_line(p.L2)
-        if l1 not in self._down:
-            self._down[l1] = compress(self.down(l1 + 1), p.row_sites(self.conf, l1, flip=True), p.cut)
-        return self._down[l1]
+        return self._line(self._down, l1, p.L1, p.L2, lambda: self.down_q(l1 + 1),
+                          lambda: p.row_sites(self.conf, l1, flip=True), lambda: p.row_q(self.conf, l1, flip=True))
+
+    def left_q(self, l2):
+        p = self.peps
+        return self._line(self._left, l2, -1, p.L1, lambda: self.left_q(l2 - 1), lambda: p.col_sites(self.conf, l2),
+                          lambda: p.col_q(self.conf, l2))
+
+    def right_q(self, l2):
+        p = self.peps
+        return self._line(self._right, l2, p.L2, p.L1, lambda: self.right_q(l2 + 1),
+                          lambda: p.col_sites(self.conf, l2, flip=True), lambda: p.col_q(self.conf, l2, flip=True))
+
+    def up(self, l1):
+        return self.up_q(l1)[0]
+
+    def down(self, l1):
+        return self.down_q(l1)[0]
 
     def left(self, l2):
-        p = self.peps
-        if l2 == -1:
-            return ones_line(p.L1)
-        if l2 not in self._left:
-            self._left[l2] = compress(self.left(l2 - 1), p.col_sites(self.conf, l2), p.cut)
-        return self._left[l2]
+        return self.left_q(l2)[0]
 
     def right(self, l2):
-        p = self.peps
-        if l2 == p.L2:
-            return ones_line(p.L1)
-        if l2 not in self._right:
-            self._right[l2] = compress(self.right(l2 + 1), p.col_sites(self.conf, l2, flip=True), p.cut)
-        return self._right[l2]
+        return self.right_q(l2)[0]
 
     # strips -------------------------------------------------------------------------------
     def row_envs(self, l1):
@@ -305,11 +427,14 @@ class SweepChain:
         self.order = sweep_order(peps)
         self.accepts = 0
         self.proposals = 0
+        self.env = None
 
     def sweep(self):
         """``SweepSampling.__call__``: returns (possibility, configuration copy)."""
         peps = self.peps
-        env = Environment(peps, self.conf)
+        if self.env is None:
+            self.env = Environment(peps, self.conf)
+        env = self.env
         ws = env.amplitude()
         for ti in self.order:
             positions, table = peps.terms[ti]
@@ -331,19 +456,21 @@ class SweepChain:
                     self.accepts += 1
                     for pos, v in zip(positions, s_new):
                         self.conf[pos[0], pos[1]] = v
-                    env = Environment(peps, self.conf)
+                    env.update([(pos[0], pos[1], v) for pos, v in zip(positions, s_new)])
         return abs(ws)**2, self.conf.copy()
 
 
 # ----------------------------------------------------------------------------------------------
 # observer
 # ----------------------------------------------------------------------------------------------
-def observe(peps, conf):
+def observe(peps, conf, env=None):
     """Per-sample quantities of ``Observer.__call__`` (observer.py:313-415).
 
     Returns (ws, eloc, holes) with ``holes[l1][l2]`` of shape (u, d, l, r) already divided by
-    ws (the sampled physical slice of ``Configuration.holes``)."""
-    env = Environment(peps, np.asarray(conf))
+    ws (the sampled physical slice of ``Configuration.holes``).  ``env``: the sampler's cached
+    environment of the same configuration, if any."""
+    if env is None or not np.array_equal(env.conf, conf):
+        env = Environment(peps, np.asarray(conf))
     ws = env.amplitude()
     eloc = 0.0
     for positions, table in peps.terms:
@@ -376,9 +503,9 @@ class ObserverAccumulator:
         self.Delta = [[np.zeros_like(peps.A[l1][l2]) for l2 in range(peps.L2)] for l1 in range(peps.L1)]
         self.EDelta = [[np.zeros_like(peps.A[l1][l2]) for l2 in range(peps.L2)] for l1 in range(peps.L1)]
 
-    def add(self, possibility, conf):
+    def add(self, possibility, conf, env=None):
         self.count += 1
-        ws, eloc, holes = observe(self.peps, conf)
+        ws, eloc, holes = observe(self.peps, conf, env)
         if ws == 0.0:
             return ws, None, holes
         reweight = ws * ws / possibility

@@ -25,10 +25,25 @@ def test_distributions_edge_cases():
     assert min(r) >= 0.0 and max(r) < 1.0
 
 
+def golden_charges(g):
+    """(legs, phys, flux) of a golden case from the reference's edge segments."""
+    from tnsp_gb300.lattice import site_charges
+    legs = [[None] * g.L2 for _ in range(g.L1)]
+    flux = [[0] * g.L2 for _ in range(g.L1)]
+    phys = None
+    for l1 in range(g.L1):
+        for l2 in range(g.L2):
+            meta = g.meta["sites"][f"{l1},{l2}"]
+            legs[l1][l2], phys, flux[l1][l2] = site_charges([m["name"] for m in meta],
+                                                            [[tuple(x) for x in m["segments"]] for m in meta])
+    return legs, phys, flux
+
+
+@pytest.mark.parametrize("charged", [False, True])
 @pytest.mark.parametrize("name", CASES)
-def test_oracle_matches_reference(name):
+def test_oracle_matches_reference(name, charged):
     g = Golden(name)
-    peps = DensePEPS(g.dense_sites(), g.terms(), g.cut)
+    peps = DensePEPS(g.dense_sites(), g.terms(), g.cut, golden_charges(g) if charged else None)
     order = [peps.terms[i][0] for i in sweep_order(peps)]
     assert order == [tuple(tuple(p) for p in ps) for ps in g.meta["sweep_order"]]
     acc = ObserverAccumulator(peps)
@@ -42,7 +57,7 @@ def test_oracle_matches_reference(name):
             assert abs(poss / z["possibility"][ci][k] - 1) < 1e-10
             if k >= g.meta["n_therm"]:
                 j = k - g.meta["n_therm"]
-                ws, eloc, holes = acc.add(poss, conf)
+                ws, eloc, holes = acc.add(poss, conf, chain.env)
                 assert abs(ws / z["ws"][ci][j] - 1) < 1e-10
                 assert abs(eloc - z["eloc"][ci][j]) < 1e-10
                 for l1 in range(g.L1):

@@ -764,7 +764,8 @@ template <class T> struct Engine : Chain<T> {
         this->count(2, 4.0 * mm * mm * nn + 8.0 * mm * nn * nn + 9.0 * nn * nn * nn);
       }
       __syncthreads();
-      const int sweeps = block_jacobi_multi<T, kMaxSec>(ns, s_nvv, s_lenv, s_xp, s_vp, kMaxSweepsJacobi);
+      const int sweeps = ns == 1 ? block_jacobi(s_nvv[0], s_lenv[0], s_xp[0], s_vp[0], kMaxSweepsJacobi)
+                                 : block_jacobi_multi<T, kMaxSec>(ns, s_nvv, s_lenv, s_xp, s_vp, kMaxSweepsJacobi);
       if (sweeps < 0 && threadIdx.x == 0) atomicOr(status, ST_SVD_NOCONV);
       {
         const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
@@ -1188,6 +1189,9 @@ __device__ void single_term(Engine<T>& eng, const Model& md, int kind, int idx, 
 template <class T>
 __global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Slots sl, T* scratch, const T* ones,
                                                          int nsweeps, int observe, int rec_base) {
+  // nsweeps == 0 with observe: observe the current configurations once, without sweeping
+  const bool observe_only = nsweeps == 0 && observe;
+  const int nsteps = observe_only ? 1 : nsweeps;
   __shared__ short s_conf[kMaxSites];
   __shared__ unsigned char s_valid[4 * kMaxL];
   __shared__ int s_eE[kMaxL + 1], s_eF[kMaxL + 1];
@@ -1224,7 +1228,7 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Sl
     }
     __syncthreads();
     uint64_t* mt = ch.mt + (long long)b * kMtN;
-    for (int sw = 0; sw < nsweeps; ++sw) {
+    for (int sw = 0; sw < nsteps; ++sw) {
       // ws = hole(())  (sampling.py:146-148)
       {
         double m;
@@ -1240,7 +1244,7 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Sl
         __syncthreads();
       }
       // horizontal bonds, row-major (sampling.py:159-177)
-      for (int l1 = 0; l1 < md.L1; ++l1) {
+      for (int l1 = 0; l1 < md.L1 && !observe_only; ++l1) {
         bool any = false;
         for (int l2 = 0; l2 + 1 < md.L2; ++l2) any |= md.hterm[l1 * md.L2 + l2] >= 0;
         if (!any) continue;
@@ -1252,7 +1256,7 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Sl
         }
       }
       // vertical bonds, column-major (sampling.py:178-186)
-      for (int l2 = 0; l2 < md.L2; ++l2) {
+      for (int l2 = 0; l2 < md.L2 && !observe_only; ++l2) {
         bool any = false;
         for (int l1 = 0; l1 + 1 < md.L1; ++l1) any |= md.vterm[l1 * md.L2 + l2] >= 0;
         if (!any) continue;

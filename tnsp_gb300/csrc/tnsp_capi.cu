@@ -523,14 +523,15 @@ int tnsp_sweep(tnsp_ctx* ctx, int nsweeps, int observe) {
   CK(cudaSetDevice(ctx->device));
   int r = ensure_slots(ctx);
   if (r) return r;
+  const int nrec = (nsweeps == 0 && observe) ? 1 : nsweeps;
   if (observe) {
     // the per-sample record holds the samples of this call
-    if (ctx->rec_cap < nsweeps) {
+    if (ctx->rec_cap < nrec) {
       dfree(ctx->d_rec);
-      CK(cudaMalloc((void**)&ctx->d_rec, sizeof(double) * 3 * (size_t)std::max(1, nsweeps) * ctx->B));
-      ctx->rec_cap = std::max(1, nsweeps);
+      CK(cudaMalloc((void**)&ctx->d_rec, sizeof(double) * 3 * (size_t)std::max(1, nrec) * ctx->B));
+      ctx->rec_cap = std::max(1, nrec);
     }
-    ctx->rec_n = nsweeps;
+    ctx->rec_n = nrec;
   }
   Model md = make_model(ctx);
   Chains ch = make_chains(ctx);
@@ -539,7 +540,7 @@ int tnsp_sweep(tnsp_ctx* ctx, int nsweeps, int observe) {
   }
   const int grid = ctx->nslots;
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
-  if (nsweeps > 0) {
+  if (nrec > 0) {
     if (ctx->precision == TNSP_FP64)
       launch_sweep_f64(grid, ctx->smem_bytes, ctx->stream, md, ch, ctx->slots, ctx->d_scratch, ctx->d_ones, nsweeps,
                        observe, 0);
@@ -553,7 +554,7 @@ int tnsp_sweep(tnsp_ctx* ctx, int nsweeps, int observe) {
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   ctx->last_ms = ms;
-  ctx->last_launches = nsweeps > 0 ? 1 : 0;
+  ctx->last_launches = nrec > 0 ? 1 : 0;
   int32_t st = 0;
   CK(cudaMemcpy(&st, ctx->d_status, sizeof(int32_t), cudaMemcpyDeviceToHost));
   if (st & (TNSP_ST_SVD_NOCONV | TNSP_ST_NONFINITE | TNSP_ST_UNSUPPORTED)) {
