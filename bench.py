@@ -33,8 +33,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOADS = {
-    "heis4x4": dict(L1=4, L2=4, D=4, sectors=None, cut=16, scale=True, chains=1024, therm=64),
-    "heis8x8u1": dict(L1=8, L2=8, D=6, sectors=(2, 2, 2), cut=36, scale=False, chains=456, therm=2),
+    "heis4x4": dict(L1=4, L2=4, D=4, sectors=None, cut=16, scale=True, chains=1024, therm=64, steps=5,
+                    precision="fp64"),
+    "heis8x8u1": dict(L1=8, L2=8, D=6, sectors=(2, 2, 2), cut=36, scale=False, chains=456, therm=2, steps=2,
+                      precision="fp32"),
 }
 DEFAULT_WORKLOAD = "heis8x8u1"
 FP64_NOMINAL_GFLOPS = 1250.0
@@ -90,6 +92,9 @@ def _cpu_worker(args):
 def cpu_baseline(workload, seconds, cores=None):
     import multiprocessing as mp
     cores = cores or min(os.cpu_count() or 1, 16)
+    # one BLAS thread per process: the spawned workers inherit these before importing numpy
+    for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[var] = "1"
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(cores) as pool:
@@ -357,16 +362,19 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=0, help="timed steps (default: per workload)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--precision", default="", choices=["", "fp64", "fp32"], help="default: per workload")
     ap.add_argument("--chains", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--quick-therm", action="store_true")
     args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    args.steps = args.steps or w["steps"]
+    args.precision = args.precision or w["precision"]
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":
