@@ -103,6 +103,7 @@ inline void plan_slots(const tnsp_ctx* c, Slots& s) {
   s.o_tau = take(chi);
   s.o_X = take(chi * chi);
   s.o_V = take(chi * chi);
+  s.o_W = take(2 * chi * chi);
   s.o_sig = take(chi);
   s.o_E = take((Lmax + 1) * s.capE);
   s.o_F = take((Lmax + 1) * s.capE);

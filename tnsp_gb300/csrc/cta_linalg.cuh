@@ -201,11 +201,12 @@ __device__ int block_jacobi(int nv, int len, T* X, T* Vr, int max_sweeps) {
   if (nv < 2) return 0;
   const int np = nv + (nv & 1);  // padded to even; index nv is a dummy
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  // Relative orthogonality target eps*len.  A vector whose squared norm is below
-  // (eps*len)^2 * max_j |x_j|^2 is rounding noise (a numerically zero singular value, which the
-  // callers discard); pairs involving one are not rotated, which keeps graded noise-vs-signal
-  // pairs from oscillating at the tolerance.
-  const T tol = Eps<T>::value() * (T)len;
+  // Relative orthogonality target eps*max(len, 32) (rounding of a dot product of short vectors
+  // would otherwise hover at the target).  A vector whose squared norm is below tol^2 *
+  // max_j |x_j|^2 is rounding noise (a numerically zero singular value, which the callers
+  // discard); pairs involving one are not rotated, which keeps graded noise-vs-signal pairs from
+  // oscillating at the tolerance.
+  const T tol = Eps<T>::value() * (T)(len > 32 ? len : 32);
   __shared__ T s_red[kWarps];
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
     T mx = 0;
@@ -423,7 +424,7 @@ __device__ int block_jacobi_multi(int ns, const int* nv, const int* len, T* cons
   if (threadIdx.x == 0) {
     int pp = 0;
     for (int t = 0; t < ns; ++t) {
-      const T tol = Eps<T>::value() * (T)len[t];
+      const T tol = Eps<T>::value() * (T)(len[t] > 32 ? len[t] : 32);
       s_noise[t] = s_noise[t] * tol * tol;
       s_np[t] = nv[t] + (nv[t] & 1);
       s_pp[t] = pp;
@@ -461,7 +462,7 @@ __device__ int block_jacobi_multi(int ns, const int* nv, const int* len, T* cons
       a = warp_sum(a);
       b = warp_sum(b);
       c2 = warp_sum(c2);
-      const T tol = Eps<T>::value() * (T)L;
+      const T tol = Eps<T>::value() * (T)(L > 32 ? L : 32);
       if (a <= s_noise[t] || b <= s_noise[t]) continue;
       if (!(fabs(c2) > tol * sqrt(a) * sqrt(b))) continue;
       if (lane == 0) s_rot[t] = 1;
@@ -512,6 +513,111 @@ __device__ int block_jacobi_multi(int ns, const int* nv, const int* len, T* cons
   const int fail = s_fail;
   __syncthreads();
   return fail ? -1 : mx;
+}
+
+
+// ---------------------------------------------------------------------------------------------
+// Householder QR with column pivoting (column-major), the preconditioner of the Jacobi SVD
+// ---------------------------------------------------------------------------------------------
+// G: m x n column-major (m >= n).  At step j the remaining column of largest norm (rows j..m) is
+// swapped into position j (ties to the lower index); perm[j] records the original column.  On exit
+// R is in the upper triangle and the reflectors below it, as in block_geqrf_cm.
+template <class T> __device__ void block_geqp3_cm(int m, int n, T* G, T* tau, int* perm, T* red) {
+  __shared__ T s_beta, s_tau, s_scale;
+  __shared__ int s_piv;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) perm[j] = j;
+  __syncthreads();
+  for (int j = 0; j < n; ++j) {
+    // pivot: largest trailing column norm (warp per column, thread 0 picks)
+    if (threadIdx.x == 0) s_piv = j;
+    __syncthreads();
+    {
+      __shared__ T s_best[kWarps];
+      __shared__ int s_bidx[kWarps];
+      T best = -1;
+      int bidx = j;
+      for (int c = j + w; c < n; c += kWarps) {
+        const T* gc = G + (long)c * m;
+        T a = 0;
+        for (int r = j + lane; r < m; r += 32) a = fma(gc[r], gc[r], a);
+        a = warp_sum(a);
+        if (a > best) {
+          best = a;
+          bidx = c;
+        }
+      }
+      if (lane == 0) {
+        s_best[w] = best;
+        s_bidx[w] = bidx;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        T b = -1;
+        int bi = j;
+        for (int k = 0; k < kWarps; ++k)
+          if (s_best[k] > b || (s_best[k] == b && s_bidx[k] < bi)) {
+            b = s_best[k];
+            bi = s_bidx[k];
+          }
+        s_piv = bi;
+      }
+      __syncthreads();
+    }
+    const int p = s_piv;
+    if (p != j) {
+      T* gj = G + (long)j * m;
+      T* gp = G + (long)p * m;
+      for (int r = threadIdx.x; r < m; r += blockDim.x) {
+        const T t = gj[r];
+        gj[r] = gp[r];
+        gp[r] = t;
+      }
+      if (threadIdx.x == 0) {
+        const int t = perm[j];
+        perm[j] = perm[p];
+        perm[p] = t;
+      }
+      __syncthreads();
+    }
+    // Householder step j (as block_geqrf_cm)
+    T* gj = G + (long)j * m;
+    T part = 0;
+    for (int r = j + 1 + threadIdx.x; r < m; r += blockDim.x) part = fma(gj[r], gj[r], part);
+    const T sigma = block_sum(part, red);
+    if (threadIdx.x == 0) {
+      const T alpha = gj[j];
+      if (sigma == (T)0) {
+        s_tau = 0;
+        s_beta = alpha;
+        s_scale = 0;
+      } else {
+        T beta = sqrt(alpha * alpha + sigma);
+        if (alpha > 0) beta = -beta;
+        s_tau = (beta - alpha) / beta;
+        s_scale = (T)1 / (alpha - beta);
+        s_beta = beta;
+      }
+      tau[j] = s_tau;
+    }
+    __syncthreads();
+    const T tj = s_tau, sc = s_scale;
+    if (tj != (T)0)
+      for (int r = j + 1 + threadIdx.x; r < m; r += blockDim.x) gj[r] *= sc;
+    __syncthreads();
+    if (threadIdx.x == 0) gj[j] = s_beta;
+    if (tj != (T)0) {
+      for (int c = j + 1 + w; c < n; c += kWarps) {
+        T* gc = G + (long)c * m;
+        T d = lane == 0 ? gc[j] : (T)0;
+        for (int r = j + 1 + lane; r < m; r += 32) d = fma(gj[r], gc[r], d);
+        d = warp_sum(d) * tj;
+        if (lane == 0) gc[j] -= d;
+        for (int r = j + 1 + lane; r < m; r += 32) gc[r] -= d * gj[r];
+      }
+    }
+    __syncthreads();
+  }
 }
 
 }  // namespace tnsp

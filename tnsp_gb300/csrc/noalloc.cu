@@ -108,7 +108,7 @@ extern "C" int tnsp_amplitude_noalloc(int L1, int L2, int P, const int* dims, co
                       + align256(sizeof(int) * (size_t)P)            // physical charges (zero)
                       + align256(sizeof(int) * (size_t)ns);          // site flux (zero)
   const size_t scratch_slot = align256((size_t)s.stride * sizeof(double));
-  const size_t ints_slot = sizeof(int) * ((size_t)4 * kMaxL * kMaxL * 3 + 4 * kMaxL + (size_t)cut * Dmax +
+  const size_t ints_slot = sizeof(int) * ((size_t)4 * kMaxL * kMaxL * 3 + 4 * kMaxL + (size_t)cut * (Dmax + 1) +
                                           (size_t)4 * kMaxL * kMaxL * 2 * cut + 4 * kMaxL * kMaxL +
                                           (size_t)kMaxL * 3 * chi + kMaxL + (size_t)(chi * Dmax + chi));
   const size_t per_slot = scratch_slot + ints_slot;
@@ -144,7 +144,7 @@ extern "C" int tnsp_amplitude_noalloc(int L1, int L2, int P, const int* dims, co
   double* d_scratch = (double*)carve(scratch_slot * nslots);
   s.ldims = (int*)carve(sizeof(int) * 4 * kMaxL * kMaxL * 3 * (size_t)nslots);
   s.lexp = (int*)carve(sizeof(int) * 4 * kMaxL * (size_t)nslots);
-  s.order = (int*)carve(sizeof(int) * (size_t)cut * Dmax * nslots);
+  s.order = (int*)carve(sizeof(int) * (size_t)cut * (Dmax + 1) * nslots);
   s.lq = (int*)carve(sizeof(int) * (size_t)4 * kMaxL * kMaxL * 2 * cut * nslots);
   s.lfl = (int*)carve(sizeof(int) * (size_t)4 * kMaxL * kMaxL * nslots);
   s.tq = (int*)carve(sizeof(int) * (size_t)kMaxL * 3 * chi * nslots);

@@ -33,6 +33,8 @@ constexpr int kMaxChi = 1024;   // cut * Dmax
 constexpr int kCounters = 16;   // per-slot counters: 4 flop classes + 12 phase cycle counters
 enum { PH_TWOLINE = 0, PH_SECTORS, PH_QR, PH_RABSORB, PH_JACOBI, PH_SVDOUT, PH_USABSORB, PH_STRIP, PH_HOLE,
        PH_OBSERVE, PH_NORMALIZE, PH_OTHER };
+// counter slots 12..15 (phases HOLE, NORMALIZE, OTHER are not timed) hold event counts
+enum { CT_COMPRESS = 12, CT_JACOBI_CALLS = 14, CT_JACOBI_SWEEPS = 15 };
 
 enum { ST_SVD_NOCONV = 1, ST_NONFINITE = 2, ST_UNSUPPORTED = 4, ST_ZERO_WS = 8 };
 enum { F_UP = 0, F_DOWN = 1, F_LEFT = 2, F_RIGHT = 3 };
@@ -78,10 +80,10 @@ struct Slots {
   long long stride;         // elements of T per slot
   long long o_lines[4];     // line storage per family: [line][site][capB]
   long long capB, capT, capR, capE, capS, capH;
-  long long o_T, o_R, o_tau, o_X, o_V, o_sig, o_E, o_F, o_t1, o_t2, o_w0, o_w1, o_h;
+  long long o_T, o_R, o_tau, o_X, o_V, o_W, o_sig, o_E, o_F, o_t1, o_t2, o_w0, o_w1, o_h;
   int* ldims;               // [slot][4][kMaxL][kMaxL][3]
   int* lexp;                // [slot][4][kMaxL]
-  int* order;               // [slot][cut*Dmax]
+  int* order;               // [slot][cut*(Dmax+1)]: kept singular values, then pivots
   double* delta;            // [slot][n_params]
   double* edelta;           // [slot][n_params]
   double* contrib;          // [slot][n_terms]
@@ -516,6 +518,7 @@ template <class T> struct Engine : Chain<T> {
   // svd.hpp:259-532); the SVD truncation keeps the `cut` largest singular values over all
   // sectors (svd.hpp:429-470).  Without symmetry every charge is zero: one sector.
   __device__ void compress(int f, int idx) {
+    this->count(CT_COMPRESS, 1.0);
     const int n = nsites_along(f);
     const int prev = (f == F_UP || f == F_LEFT) ? idx - 1 : idx + 1;
     const int orient = f;  // 0: UDLR, 1: DULR, 2: LRUD, 3: RLUD
@@ -726,25 +729,36 @@ template <class T> struct Engine : Chain<T> {
       int S = 0;
       for (int t = 0; t < ns; ++t) S += min(s_sec.m[t], s_sec.c[t]);
       const T* M = Tbuf(s_buf[i]);
-      // gather every sector's vectors (columns when the block is tall, rows when wide); sectors are
-      // staged in shared memory while it has room, the others work in the slot's X/V arrays
+      // QR-preconditioned one-sided Jacobi (Drmac-Veselic): per sector, A (len x nv, its columns are
+      // the block's columns when it is tall, its rows when wide) = Q R P^T by Householder QR with
+      // column pivoting, then one-sided Jacobi on the nv columns of R^T (accumulating J), which
+      // converges in fewer sweeps and on vectors of length nv.  With B = R^T, B J = W:
+      //   A = (Q J) Sigma (P W Sigma^-1)^T,  sigma_j = |W_j|.
+      // Outputs per kept value j: lenvec_j = (Q J)_j (len-dim, unit) and nvvec_j = P W_j (nv-dim,
+      // sigma_j times unit).  Sector data sit in shared memory while it has room, else in the slot.
       __shared__ int s_nvv[kMaxSec], s_lenv[kMaxSec];
-      __shared__ T* s_xp[kMaxSec];
-      __shared__ T* s_vp[kMaxSec];
+      __shared__ T* s_xp[kMaxSec];  // A, then Q (len x nv, column-major)
+      __shared__ T* s_bp[kMaxSec];  // B = R^T vectors, rotated into W (nv x nv)
+      __shared__ T* s_jp[kMaxSec];  // J (nv x nv)
+      T* Wl = slot + sl.o_W;                         // lenvec, packed at s_xo
+      T* Wn = slot + sl.o_W + (long long)chi() * chi();  // nvvec, packed at s_vo
+      int* perm = order + md.cut;                    // pivots of the current sector (<= chi entries)
       if (threadIdx.x == 0) {
         long long used = 0;
         for (int t = 0; t < ns; ++t) {
           const int nv = min(s_sec.m[t], s_sec.c[t]), len = max(s_sec.m[t], s_sec.c[t]);
           s_nvv[t] = nv;
           s_lenv[t] = len;
-          const long long need = (long long)nv * len + (long long)nv * nv;
+          const long long need = (long long)nv * len + 2LL * nv * nv;
           if (used + need <= smcap) {
             s_xp[t] = sm + used;
-            s_vp[t] = sm + used + (long long)nv * len;
+            s_bp[t] = sm + used + (long long)nv * len;
+            s_jp[t] = sm + used + (long long)nv * len + (long long)nv * nv;
             used += need;
           } else {
             s_xp[t] = X + s_xo[t];
-            s_vp[t] = V + s_vo[t];
+            s_bp[t] = V + s_vo[t];
+            s_jp[t] = Rb + s_vo[t];
           }
         }
       }
@@ -764,32 +778,74 @@ template <class T> struct Engine : Chain<T> {
         this->count(2, 4.0 * mm * mm * nn + 8.0 * mm * nn * nn + 9.0 * nn * nn * nn);
       }
       __syncthreads();
-      const int sweeps = ns == 1 ? block_jacobi(s_nvv[0], s_lenv[0], s_xp[0], s_vp[0], kMaxSweepsJacobi)
-                                 : block_jacobi_multi<T, kMaxSec>(ns, s_nvv, s_lenv, s_xp, s_vp, kMaxSweepsJacobi);
+      // QR with column pivoting per sector; B = R^T as nv vectors of length nv (vector i = row i of R)
+      for (int t = 0; t < ns; ++t) {
+        const int nv = s_nvv[t], len = s_lenv[t];
+        T* x = s_xp[t];
+        block_geqp3_cm(len, nv, x, tau + 0, perm, red);
+        T* b = s_bp[t];
+        for (long long e = threadIdx.x; e < (long long)nv * nv; e += blockDim.x) {
+          const int i = (int)(e / nv), k = (int)(e % nv);
+          b[e] = k >= i ? x[(long long)k * len + i] : (T)0;
+        }
+        // keep the pivots and reflector scalars of this sector next to its J block (J is set up by
+        // the Jacobi routine later): store them in the packed nvvec area, which is written last
+        int* pk = reinterpret_cast<int*>(Wn + s_vo[t]);
+        T* tk = Wl + s_xo[t];
+        for (int k = threadIdx.x; k < nv; k += blockDim.x) {
+          pk[k] = perm[k];
+          tk[k] = tau[k];
+        }
+        __syncthreads();
+      }
+      const int sweeps = ns == 1 ? block_jacobi(s_nvv[0], s_nvv[0], s_bp[0], s_jp[0], kMaxSweepsJacobi)
+                                 : block_jacobi_multi<T, kMaxSec>(ns, s_nvv, s_nvv, s_bp, s_jp, kMaxSweepsJacobi);
       if (sweeps < 0 && threadIdx.x == 0) atomicOr(status, ST_SVD_NOCONV);
+      this->count(CT_JACOBI_CALLS, 1.0);
+      this->count(CT_JACOBI_SWEEPS, (double)(sweeps > 0 ? sweeps : 0));
       {
         const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
         for (int t = 0; t < ns; ++t) {
-          const int nv = s_nvv[t], len = s_lenv[t];
-          const T* x = s_xp[t];
+          const int nv = s_nvv[t];
+          const T* b = s_bp[t];
           for (int j = wp; j < nv; j += kWarps) {
             T s2 = 0;
-            for (int q = lane; q < len; q += 32) s2 = fma(x[(long long)j * len + q], x[(long long)j * len + q], s2);
+            for (int q = lane; q < nv; q += 32) s2 = fma(b[(long long)j * nv + q], b[(long long)j * nv + q], s2);
             s2 = warp_sum(s2);
             if (lane == 0) sig[s_so[t] + j] = sqrt(s2);
           }
         }
       }
-      // results of shared-memory sectors back to the packed X/V arrays read by the output stage
-      for (int t = 0; t < ns; ++t) {
-        if (s_xp[t] == X + s_xo[t]) continue;
-        const int nv = s_nvv[t], len = s_lenv[t];
-        for (long long e = threadIdx.x; e < (long long)nv * len; e += blockDim.x) X[s_xo[t] + e] = s_xp[t][e];
-        for (long long e = threadIdx.x; e < (long long)nv * nv; e += blockDim.x) V[s_vo[t] + e] = s_vp[t][e];
-      }
       __syncthreads();
-      toc(PH_JACOBI, t0);
-      t0 = tic();
+      // per sector: Q from the reflectors, lenvec = Q J, nvvec = P W
+      for (int t = 0; t < ns; ++t) {
+        const int nv = s_nvv[t], len = s_lenv[t];
+        T* x = s_xp[t];
+        int* pk = reinterpret_cast<int*>(Wn + s_vo[t]);
+        T* tk = Wl + s_xo[t];
+        for (int k = threadIdx.x; k < nv; k += blockDim.x) {
+          perm[k] = pk[k];
+          tau[k] = tk[k];
+        }
+        __syncthreads();
+        block_orgqr_cm(len, nv, x, tau);
+        const T* J = s_jp[t];
+        const T* b = s_bp[t];
+        T* lv = Wl + s_xo[t];
+        T* nvv = Wn + s_vo[t];
+        for (long long e = threadIdx.x; e < (long long)nv * len; e += blockDim.x) {
+          const int j = (int)(e / len), q = (int)(e % len);
+          const T* Jj = J + (long long)j * nv;
+          T acc = 0;
+          for (int k = 0; k < nv; ++k) acc = fma(x[(long long)k * len + q], Jj[k], acc);
+          lv[e] = acc;
+        }
+        for (long long e = threadIdx.x; e < (long long)nv * nv; e += blockDim.x) {
+          const int j = (int)(e / nv), k = (int)(e % nv);
+          nvv[(long long)j * nv + perm[k]] = b[e];
+        }
+        __syncthreads();
+      }
       const int c = md.cut < S ? md.cut : S;
       // global selection: descending value, ties to the earlier sector / lower index
       for (int j = threadIdx.x; j < S; j += blockDim.x) {
@@ -829,14 +885,15 @@ template <class T> struct Engine : Chain<T> {
         const bool caseA = mc <= mr;
         const int nv = caseA ? mc : mr, len = caseA ? mr : mc;
         const T sv = sig[s_so[t] + j];
-        const T* xj = X + s_xo[t] + (long long)j * len;
-        const T* vj = V + s_vo[t] + (long long)j * nv;
+        const T* lj = Wl + s_xo[t] + (long long)j * len;   // unit, len-dim
+        const T* nj = Wn + s_vo[t] + (long long)j * nv;    // sigma * unit, nv-dim
+        // tall block (case A): columns are the nv side; wide block: rows are the nv side
         if (q < mc) {  // right singular vector component at column C[q]
-          const T val = caseA ? vj[q] : (sv > thr ? xj[q] / sv : (T)0);
+          const T val = caseA ? (sv > thr ? nj[q] / sv : (T)0) : lj[q];
           Tn[(long long)k * cols + cl[s_sec.co[t] + q]] = val;
         }
         if (q < mr) {  // U*S component at row R[q]
-          const T val = caseA ? xj[q] : (sv > thr ? vj[q] * sv : (T)0);
+          const T val = caseA ? lj[q] * sv : nj[q];
           Rb[(long long)rl[s_sec.ro[t] + q] * c + k] = val;
         }
       }
@@ -1207,7 +1264,7 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Sl
   const int nsite = md.L1 * md.L2;
   Engine<T> eng{{md, sl, scratch + (long long)blockIdx.x * sl.stride, (const T*)md.A,
                  sl.ldims + (long long)blockIdx.x * 4 * kMaxL * kMaxL * 3, sl.lexp + (long long)blockIdx.x * 4 * kMaxL,
-                 sl.order + (long long)blockIdx.x * md.cut * md.Dmax, s_conf, s_valid, s_eE, s_eF, s_red, s_dred, s_fl},
+                 sl.order + (long long)blockIdx.x * md.cut * (md.Dmax + 1), s_conf, s_valid, s_eE, s_eF, s_red, s_dred, s_fl},
                 ones, ch.status};
   eng.strip_kind = &s_strip_kind;
   eng.strip_idx = &s_strip_idx;
@@ -1415,7 +1472,7 @@ __global__ void __launch_bounds__(kThreads) amplitude_kernel(Model md, Slots sl,
   const int nsite = md.L1 * md.L2;
   Engine<T> eng{{md, sl, scratch + (long long)blockIdx.x * sl.stride, (const T*)md.A,
                  sl.ldims + (long long)blockIdx.x * 4 * kMaxL * kMaxL * 3, sl.lexp + (long long)blockIdx.x * 4 * kMaxL,
-                 sl.order + (long long)blockIdx.x * md.cut * md.Dmax, s_conf, s_valid, s_eE, s_eF, s_red, s_dred, s_fl},
+                 sl.order + (long long)blockIdx.x * md.cut * (md.Dmax + 1), s_conf, s_valid, s_eE, s_eF, s_red, s_dred, s_fl},
                 ones, status};
   eng.strip_kind = &s_strip_kind;
   eng.strip_idx = &s_strip_idx;

@@ -167,7 +167,7 @@ int ensure_slots(tnsp_ctx* ctx) {
   CK(cudaMalloc(&ctx->d_ones, 16));
   CK(cudaMalloc((void**)&ctx->d_ldims, sizeof(int) * 4 * kMaxL * kMaxL * 3 * ctx->nslots));
   CK(cudaMalloc((void**)&ctx->d_lexp, sizeof(int) * 4 * kMaxL * ctx->nslots));
-  CK(cudaMalloc((void**)&ctx->d_order, sizeof(int) * ctx->cut * ctx->Dmax * ctx->nslots));
+  CK(cudaMalloc((void**)&ctx->d_order, sizeof(int) * ctx->cut * (ctx->Dmax + 1) * ctx->nslots));
   CK(cudaMalloc((void**)&ctx->d_delta, sizeof(double) * ctx->n_params * ctx->nslots));
   CK(cudaMalloc((void**)&ctx->d_edelta, sizeof(double) * ctx->n_params * ctx->nslots));
   CK(cudaMalloc((void**)&ctx->d_contrib, sizeof(double) * std::max(1, ctx->n_terms) * ctx->nslots));
