@@ -8,6 +8,7 @@ series (pooled autocorrelation, Sokal window c=5).
 Workloads (seeded synthetic PEPS, no dataset involved):
   heis4x4    4x4 Heisenberg (J=1), no symmetry, D=4, Dcut=16, tensors N(0,1)/sqrt(2 D^z),
              Neel start, 64 thermalisation sweeps, 1024 chains (1024 samples per step)
+  heis6x6u1  6x6 Heisenberg, U(1) D=6, Dcut=16, 16 chains: the small case used for ncu captures
   heis8x8u1  8x8 Heisenberg, U(1) bonds {-1:2, 0:2, +1:2} (D=6), Dcut=36, blocks N(0,1),
              Neel start (total Sz = 0), 456 chains = one resident wave of 3 blocks x 152 SMs
              (the 4096-sample launch runs the same kernel for nine waves), 2 thermalisation sweeps
@@ -39,9 +40,23 @@ WORKLOADS = {
                     precision="fp64"),
     "heis8x8u1": dict(L1=8, L2=8, D=6, sectors=(2, 2, 2), cut=36, scale=False, chains=456, therm=2, steps=2,
                       precision="fp64"),
+    # a small U(1) case for kernel profiling (ncu --set full ends by itself on it)
+    "heis6x6u1": dict(L1=6, L2=6, D=6, sectors=(2, 2, 2), cut=16, scale=False, chains=16, therm=1, steps=1,
+                      precision="fp64"),
 }
 DEFAULT_WORKLOAD = "heis8x8u1"
 FP64_NOMINAL_GFLOPS = 1250.0
+# FP32 pipe: 152 SMs x 128 FMA/clk x 2 flops x 2.07 GHz; one double-float multiply-add (the sampler's
+# inner operation in TNSP_DD mode: 1 FMUL + 3 FFMA + 20 FADD) issues 24 FP32 instructions, so its flop
+# peak is 1/24 of the FP32 flop rate
+FP32_NOMINAL_GFLOPS = 152 * 128 * 2 * 2.07
+DD_FMA_INSTRUCTIONS = 24
+DD_NOMINAL_GFLOPS = FP32_NOMINAL_GFLOPS / DD_FMA_INSTRUCTIONS
+
+
+def _jsonable(o):
+    """numpy scalars and arrays in the result line"""
+    return o.tolist() if hasattr(o, "tolist") else str(o)
 
 
 def make_lattice(w, seed=20240601):
@@ -49,7 +64,8 @@ def make_lattice(w, seed=20240601):
     return random_heisenberg(w["L1"], w["L2"], w["D"], seed=seed, scale=w["scale"], sectors=w["sectors"])
 
 
-PHASE_NAMES = ("two_line", "sectors", "qr", "r_absorb", "jacobi", "svd_out", "us_absorb", "strip", None, "observe",
+# svd_other = the SVD's gather, pivoted QR, Q*J, global selection and output (everything but the Jacobi)
+PHASE_NAMES = ("two_line", "sectors", "qr", "r_absorb", "jacobi", "svd_other", "us_absorb", "strip", None, "observe",
                None, None)
 
 
@@ -191,14 +207,14 @@ def dist_setup(gpus):
 
 def run_ours(args):
     import torch
-    from tnsp_gb300.engine import Sampler, TNSP_FP32, TNSP_FP64
+    from tnsp_gb300.engine import PRECISIONS, Sampler, TNSP_DD, TNSP_FP32, TNSP_FP64
     from tnsp_gb300.lattice import neel
     rank, world, dist = dist_setup(args.gpus)
     local = int(os.environ.get("LOCAL_RANK", 0))
     w = WORKLOADS[args.workload]
     B = args.chains or w["chains"]
     lat = make_lattice(w)
-    prec = TNSP_FP32 if args.precision == "fp32" else TNSP_FP64
+    prec = PRECISIONS[args.precision]
     s = Sampler(lat, w["cut"], device=local)
     seeds = np.arange(B, dtype=np.uint64) + np.uint64(7919 * (rank + 1))
     s.init_chains(neel(lat.L1, lat.L2), seeds, precision=prec)
@@ -235,8 +251,8 @@ def run_ours(args):
         dist.barrier()
     flops = s.counters(reset=True)
     fp64_check = None
-    if prec == TNSP_FP32:
-        # the same configurations observed in float64: E_loc and energy-per-site error of float32
+    if prec != TNSP_FP64:
+        # the same configurations observed in float64: E_loc and energy-per-site error of this mode
         conf, _ = s.read_chains()
         e32 = np.asarray(elocs[-1])
         s64 = Sampler(lat, w["cut"], device=local)
@@ -267,7 +283,10 @@ def run_ours(args):
     raw = samples / t_dev
     value = raw / (2 * tau)
     e2e_raw = samples / t_e2e
-    h2d = n_params * 8 + n_params * 4 + lat.L1 * lat.L2 * 4 * 4 + int(sum(len(v) for v in lat.term_arrays()[1:]) * 4)
+    # per step: the float64 tensors, the bond extents and (U(1) lattices) the index charges
+    h2d = n_params * 8 + lat.L1 * lat.L2 * 4 * 4
+    if lat.charges is not None:
+        h2d += lat.L1 * lat.L2 * 4 * int(np.max(lat.dims())) * 4 + lat.P * 4 + lat.L1 * lat.L2 * 4
     d2h = 8 * 8 + 2 * n_params * 8 + 3 * B * 8 + 4
     avg_launch_ms = kernel_ms / args.steps
     cycles = flops[4:]
@@ -275,6 +294,16 @@ def run_ours(args):
     achieved = float(flops.sum()) / args.steps / (avg_launch_ms * 1e-3) / 1e9
     if rank != 0:
         return
+    if prec == TNSP_FP64:
+        bound, kname, peak = "fp64", "sweep_kernel<double>", FP64_NOMINAL_GFLOPS
+        peak_src = "nominal GB300 FP64 1.25 TFLOP/s (MEASURED_PEAKS.json has no FP64 figure)"
+    elif prec == TNSP_DD:
+        bound, kname, peak = "fp32 (double-float)", "sweep_kernel<dd>", DD_NOMINAL_GFLOPS
+        peak_src = (f"nominal GB300 FP32 {FP32_NOMINAL_GFLOPS:.0f} GFLOP/s / {DD_FMA_INSTRUCTIONS} FP32 instructions "
+                    "per double-float multiply-add (MEASURED_PEAKS.json has no FP32 figure)")
+    else:
+        bound, kname, peak = "fp32", "sweep_kernel<float>", FP32_NOMINAL_GFLOPS
+        peak_src = "nominal GB300 FP32 (MEASURED_PEAKS.json has no FP32 figure)"
     cpu = None
     if not args.no_cpu and world == 1:
         c = cpu_baseline(args.workload, args.cpu_seconds)
@@ -297,7 +326,7 @@ def run_ours(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64" if prec == TNSP_FP64 else "f32",
+        "dtype": {TNSP_FP64: "f64", TNSP_FP32: "f32", TNSP_DD: "f32x2 (double-float)"}[prec],
         "data": "synthetic (seeded random PEPS, Neel start)",
         "config": {"workload": args.workload, "lattice": f"{w['L1']}x{w['L2']}", "D": w["D"],
                    "sectors": w["sectors"], "Dcut": w["cut"], "chains_per_gpu": B,
@@ -312,10 +341,8 @@ def run_ours(args):
         "e2e": {"value": e2e_raw / (2 * tau), "unit": "effective samples/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": args.steps,
-        "roofline": {"bound": "fp64", "kernel": "sweep_kernel<double>" if prec == TNSP_FP64 else "sweep_kernel<float>",
-                     "achieved": achieved, "peak": FP64_NOMINAL_GFLOPS if prec == TNSP_FP64 else None,
-                     "unit": "GFLOP/s", "frac": achieved / FP64_NOMINAL_GFLOPS if prec == TNSP_FP64 else None,
-                     "peak_source": "nominal GB300 FP64 1.25 TFLOP/s (no FP64 figure in MEASURED_PEAKS.json)",
+        "roofline": {"bound": bound, "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GFLOP/s",
+                     "frac": achieved / peak if peak else None, "peak_source": peak_src,
                      "flops_per_launch": float(flops.sum()) / args.steps,
                      "flops_split": {"contract": flops[0] / args.steps, "qr": flops[1] / args.steps,
                                      "svd": flops[2] / args.steps, "strip": flops[3] / args.steps},
@@ -325,7 +352,7 @@ def run_ours(args):
         "clocks": clocks.summary(),
         "fp64_check": fp64_check,
     }
-    print(json.dumps(out))
+    print(json.dumps(out, default=_jsonable))
 
 
 def run_reference(args):
@@ -374,7 +401,7 @@ def run_reference(args):
                                    "single-threaded process (the reference itself is not installable on the GPU box)"},
         "e2e": {"value": value, "unit": "effective samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    print(json.dumps(out))
+    print(json.dumps(out, default=_jsonable))
 
 
 def main():
@@ -384,7 +411,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="", choices=["", "fp64", "fp32"], help="default: per workload")
+    ap.add_argument("--precision", default="", choices=["", "fp64", "dd", "fp32"], help="default: per workload")
     ap.add_argument("--chains", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")

@@ -33,9 +33,15 @@ extern "C" {
 
 typedef struct tnsp_ctx tnsp_ctx;
 
-/* precision of the tensor arithmetic inside the sampler */
+/* precision of the tensor arithmetic inside the sampler (ratios, exponents and every accumulator
+ * are float64 in all modes):
+ *   TNSP_FP64  float64 (the reference's arithmetic)
+ *   TNSP_FP32  float32; too coarse where amplitudes cancel strongly (large lattices)
+ *   TNSP_DD    double-float: each value is a pair of floats (hi + lo, about 2^-46 relative
+ *              precision) computed on the FP32 pipe, which GB300 runs at 64x its FP64 rate */
 #define TNSP_FP64 0
 #define TNSP_FP32 1
+#define TNSP_DD 2
 
 /*
  * Creates a context on CUDA device `device` using stream `stream` (a cudaStream_t, or NULL for

@@ -11,6 +11,8 @@ LIB_PATH = os.path.join(HERE, "libtnsp_gb300.so")
 
 TNSP_FP64 = 0
 TNSP_FP32 = 1
+TNSP_DD = 2
+PRECISIONS = {"fp64": TNSP_FP64, "fp32": TNSP_FP32, "dd": TNSP_DD}
 
 _c_int_p = ctypes.POINTER(ctypes.c_int)
 _c_i32_p = ctypes.POINTER(ctypes.c_int32)

@@ -20,7 +20,8 @@ struct tnsp_ctx {
   std::vector<long long> off;
   long long n_params = 0;
   double* dA64 = nullptr;
-  float* dA32 = nullptr;
+  float* dA32 = nullptr;           // float copy (TNSP_FP32)
+  tnsp::dd* dAdd = nullptr;        // double-float copy (TNSP_DD)
   int* d_dims = nullptr;
   long long* d_off = nullptr;
   std::vector<double> hostA;       // host copy of the site tensors (charge validation)

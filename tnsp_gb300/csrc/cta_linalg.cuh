@@ -2,11 +2,13 @@
 //
 // Every routine here is called by all threads of the block with identical arguments and ends
 // with a __syncthreads(); operands live in global memory (this block's scratch slot) and are
-// row-major unless stated.  The element type T is double (the FP64 sampler) or float (the
-// mixed sampler); reductions that decide control flow are done in the element type.
+// row-major unless stated.  The element type T is double (the FP64 sampler), dd (double-float,
+// ddfloat.cuh) or float; reductions that decide control flow are done in the element type.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include "ddfloat.cuh"
 
 namespace tnsp {
 
@@ -20,6 +22,12 @@ template <> struct Eps<double> {
 template <> struct Eps<float> {
   static __device__ __forceinline__ float value() { return 5.9604645e-08f; }
 };
+// double-float: 2^-44.  Its dot products err by up to ~2^-46 of the operands' magnitudes (float64's
+// fused multiply-add rounds once, relative to the result), so the Jacobi stopping test
+// |g| <= eps*len*sqrt(ab) needs this margin on the 216-long sector vectors of a Dcut=36, D=6 lattice
+template <> struct Eps<dd> {
+  static __device__ __forceinline__ dd value() { return dd(5.684342e-14f, 0.f); }
+};
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -31,11 +39,38 @@ __device__ __forceinline__ float warp_sum(float v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+__device__ __forceinline__ dd warp_sum(dd v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = v + shfl_xor(v, o);
+  return v;
+}
 template <class T> __device__ __forceinline__ T warp_max(T v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
 }
+__device__ __forceinline__ dd warp_max(dd v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, shfl_xor(v, o));
+  return v;
+}
+
+// Tangent of the one-sided Jacobi rotation angle, t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2)).  For
+// double-float, zeta^2 overflows float's exponent range on strongly graded pairs (|zeta| ~ 1e21 next
+// to the noise floor), which would make t = 0 and the pair never converge; above 2^40 the series
+// value t = 1 / (2 zeta) is used (relative error below zeta^-2).
+template <class T> __device__ __forceinline__ T jacobi_tan(T zeta) {
+  return (zeta >= 0 ? (T)1 : (T)-1) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
+}
+__device__ __forceinline__ dd jacobi_tan(dd zeta) {
+  if (fabs(zeta) > dd(1.0995116e12f, 0.f)) return dd(1.f, 0.f) / (dd(2.f, 0.f) * zeta);
+  return (zeta >= dd(0.f, 0.f) ? dd(1.f, 0.f) : dd(-1.f, 0.f)) / (fabs(zeta) + sqrt(dd(1.f, 0.f) + zeta * zeta));
+}
+
+// Shared-memory accumulation of a threshold estimate (order-independent to rounding only).
+__device__ __forceinline__ void shared_accumulate(double* p, double v) { atomicAdd(p, v); }
+__device__ __forceinline__ void shared_accumulate(float* p, float v) { atomicAdd(p, v); }
+__device__ __forceinline__ void shared_accumulate(dd* p, dd v) { atomicAdd(&p->hi, v.hi + v.lo); }
 
 // Block-wide sum; `red` is shared scratch of kWarps doubles.  Result broadcast to all threads.
 template <class T> __device__ T block_sum(T v, T* red) {
@@ -241,7 +276,7 @@ __device__ int block_jacobi(int nv, int len, T* X, T* Vr, int max_sweeps) {
         if (!(fabs(g) > tol * sqrt(a) * sqrt(b))) continue;
         rot = 1;
         const T zeta = (b - a) / ((T)2 * g);
-        const T t = (zeta >= 0 ? (T)1 : (T)-1) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
+        const T t = jacobi_tan(zeta);
         const T c = (T)1 / sqrt((T)1 + t * t);
         const T s = c * t;
         for (int r = lane; r < len; r += 32) {
@@ -418,7 +453,7 @@ __device__ int block_jacobi_multi(int ns, const int* nv, const int* len, T* cons
     T acc = 0;
     for (long e = threadIdx.x; e < (long)nv[t] * len[t]; e += blockDim.x) acc = fma(Xs[t][e], Xs[t][e], acc);
     acc = warp_sum(acc);
-    if (lane == 0) atomicAdd(&s_noise[t], acc);
+    if (lane == 0) shared_accumulate(&s_noise[t], acc);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -467,7 +502,7 @@ __device__ int block_jacobi_multi(int ns, const int* nv, const int* len, T* cons
       if (!(fabs(c2) > tol * sqrt(a) * sqrt(b))) continue;
       if (lane == 0) s_rot[t] = 1;
       const T zeta = (b - a) / ((T)2 * c2);
-      const T tt = (zeta >= 0 ? (T)1 : (T)-1) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
+      const T tt = jacobi_tan(zeta);
       const T c = (T)1 / sqrt((T)1 + tt * tt);
       const T sn = c * tt;
       for (int r = lane; r < L; r += 32) {

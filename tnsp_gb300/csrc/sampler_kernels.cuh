@@ -602,6 +602,11 @@ template <class T> struct Engine : Chain<T> {
           g[e] = M[(long long)R_[x] * cols + C_[y]];
         }
         __syncthreads();
+        // power-of-two scaling of the sector to max |g| in [0.5, 1): exact, so Q and R / 2^es are the
+        // factors of the unscaled block; it keeps the squared norms of a sector that is small next to
+        // the tensor's largest one inside the exponent range of float-based element types
+        const int es = block_normalize(g, (long long)mr * mc, red);
+        const T rsc = (T)ldexp(1.0, es);
         block_geqrf_cm(mr, mc, g, tau, red);
         {
           const double mm = mr > mc ? mr : mc, nn = kr;
@@ -611,7 +616,7 @@ template <class T> struct Engine : Chain<T> {
         T* rb = Rb + s_roffs[t];
         for (long long e = threadIdx.x; e < (long long)kr * mc; e += blockDim.x) {
           const int y = (int)(e / mc), z = (int)(e % mc);
-          rb[e] = z >= y ? g[(long long)z * mr + y] : (T)0;
+          rb[e] = z >= y ? g[(long long)z * mr + y] * rsc : (T)0;
         }
         __syncthreads();
         block_orgqr_cm(mr, kr, g, tau);
@@ -736,7 +741,7 @@ template <class T> struct Engine : Chain<T> {
       //   A = (Q J) Sigma (P W Sigma^-1)^T,  sigma_j = |W_j|.
       // Outputs per kept value j: lenvec_j = (Q J)_j (len-dim, unit) and nvvec_j = P W_j (nv-dim,
       // sigma_j times unit).  Sector data sit in shared memory while it has room, else in the slot.
-      __shared__ int s_nvv[kMaxSec], s_lenv[kMaxSec];
+      __shared__ int s_nvv[kMaxSec], s_lenv[kMaxSec], s_esec[kMaxSec];
       __shared__ T* s_xp[kMaxSec];  // A, then Q (len x nv, column-major)
       __shared__ T* s_bp[kMaxSec];  // B = R^T vectors, rotated into W (nv x nv)
       __shared__ T* s_jp[kMaxSec];  // J (nv x nv)
@@ -782,6 +787,9 @@ template <class T> struct Engine : Chain<T> {
       for (int t = 0; t < ns; ++t) {
         const int nv = s_nvv[t], len = s_lenv[t];
         T* x = s_xp[t];
+        // exact power-of-two scaling of the sector (as in the QR sweep); sigma and P W are scaled back
+        const int es = block_normalize(x, (long long)nv * len, red);
+        if (threadIdx.x == 0) s_esec[t] = es;
         block_geqp3_cm(len, nv, x, tau + 0, perm, red);
         T* b = s_bp[t];
         for (long long e = threadIdx.x; e < (long long)nv * nv; e += blockDim.x) {
@@ -798,8 +806,12 @@ template <class T> struct Engine : Chain<T> {
         }
         __syncthreads();
       }
+      toc(PH_SVDOUT, t0);  // gather + pivoted QR
+      t0 = tic();
       const int sweeps = ns == 1 ? block_jacobi(s_nvv[0], s_nvv[0], s_bp[0], s_jp[0], kMaxSweepsJacobi)
                                  : block_jacobi_multi<T, kMaxSec>(ns, s_nvv, s_nvv, s_bp, s_jp, kMaxSweepsJacobi);
+      toc(PH_JACOBI, t0);
+      t0 = tic();
       if (sweeps < 0 && threadIdx.x == 0) atomicOr(status, ST_SVD_NOCONV);
       this->count(CT_JACOBI_CALLS, 1.0);
       this->count(CT_JACOBI_SWEEPS, (double)(sweeps > 0 ? sweeps : 0));
@@ -808,11 +820,12 @@ template <class T> struct Engine : Chain<T> {
         for (int t = 0; t < ns; ++t) {
           const int nv = s_nvv[t];
           const T* b = s_bp[t];
+          const T ssc = (T)ldexp(1.0, s_esec[t]);
           for (int j = wp; j < nv; j += kWarps) {
             T s2 = 0;
             for (int q = lane; q < nv; q += 32) s2 = fma(b[(long long)j * nv + q], b[(long long)j * nv + q], s2);
             s2 = warp_sum(s2);
-            if (lane == 0) sig[s_so[t] + j] = sqrt(s2);
+            if (lane == 0) sig[s_so[t] + j] = sqrt(s2) * ssc;
           }
         }
       }
@@ -840,9 +853,10 @@ template <class T> struct Engine : Chain<T> {
           for (int k = 0; k < nv; ++k) acc = fma(x[(long long)k * len + q], Jj[k], acc);
           lv[e] = acc;
         }
+        const T ssc = (T)ldexp(1.0, s_esec[t]);
         for (long long e = threadIdx.x; e < (long long)nv * nv; e += blockDim.x) {
           const int j = (int)(e / nv), k = (int)(e % nv);
-          nvv[(long long)j * nv + perm[k]] = b[e];
+          nvv[(long long)j * nv + perm[k]] = b[e] * ssc;
         }
         __syncthreads();
       }

@@ -1,5 +1,6 @@
 // C ABI of the sampler (declared in include/tnsp_gb300.h): host-side plan, buffers and launches.
-// The kernels are instantiated in sampler_f64.cu / sampler_f32.cu and reached through launch.h.
+// The kernels are instantiated in sampler_f64.cu / sampler_dd.cu / sampler_f32.cu and reached
+// through launch.h.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -26,6 +27,17 @@ __global__ void reduce_slots(const double* __restrict__ src, int nslots, long lo
 
 template <class T> __global__ void fill_ones(T* p) {
   if (threadIdx.x == 0 && blockIdx.x == 0) p[0] = (T)1;
+}
+
+// float and double-float copies of the float64 site tensors (round to nearest; hi + lo carries
+// the float64 value to about 2^-48 relative)
+__global__ void convert_tensors(const double* __restrict__ a, long long n, float* __restrict__ a32,
+                                dd* __restrict__ add) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double x = a[i];
+    a32[i] = (float)x;
+    add[i] = dd(x);
+  }
 }
 }  // namespace tnsp
 
@@ -96,6 +108,7 @@ void free_model(tnsp_ctx* c) {
 void free_lattice(tnsp_ctx* c) {
   dfree(c->dA64);
   dfree(c->dA32);
+  dfree(c->dAdd);
   dfree(c->d_dims);
   dfree(c->d_off);
   dfree(c->d_qleg);
@@ -113,7 +126,9 @@ Model make_model(tnsp_ctx* c) {
   m.Dmax = c->Dmax;
   m.dims = c->d_dims;
   m.off = c->d_off;
-  m.A = c->precision == TNSP_FP64 ? (const void*)c->dA64 : (const void*)c->dA32;
+  m.A = c->precision == TNSP_FP64 ? (const void*)c->dA64
+        : c->precision == TNSP_DD  ? (const void*)c->dAdd
+                                   : (const void*)c->dA32;
   m.n_terms = c->n_terms;
   m.term_sites = c->d_term_sites;
   m.hterm = c->d_hterm;
@@ -155,7 +170,7 @@ int ensure_slots(tnsp_ctx* ctx) {
   CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
   Slots s{};
   plan_slots(ctx, s);
-  ctx->elem = ctx->precision == TNSP_FP64 ? 8 : 4;
+  ctx->elem = ctx->precision == TNSP_FP32 ? 4 : 8;
   // as many resident blocks as fit: 3 per SM, bounded by a scratch budget of 64 GB
   long long want = 3LL * sms;
   const long long per = s.stride * (long long)ctx->elem + 2LL * ctx->n_params * 8;
@@ -186,6 +201,8 @@ int ensure_slots(tnsp_ctx* ctx) {
   ctx->smem_bytes = 64 * 1024;
   if (ctx->precision == TNSP_FP64)
     CK(set_smem_limit_f64((int)ctx->smem_bytes));
+  else if (ctx->precision == TNSP_DD)
+    CK(set_smem_limit_dd((int)ctx->smem_bytes));
   else
     CK(set_smem_limit_f32((int)ctx->smem_bytes));
   CK(cudaMemsetAsync(ctx->d_flops, 0, sizeof(double) * kCounters * ctx->nslots, ctx->stream));
@@ -193,6 +210,8 @@ int ensure_slots(tnsp_ctx* ctx) {
   CK(cudaMemsetAsync(ctx->d_edelta, 0, sizeof(double) * ctx->n_params * ctx->nslots, ctx->stream));
   if (ctx->precision == TNSP_FP64)
     fill_ones<double><<<1, 32, 0, ctx->stream>>>((double*)ctx->d_ones);
+  else if (ctx->precision == TNSP_DD)
+    fill_ones<dd><<<1, 32, 0, ctx->stream>>>((dd*)ctx->d_ones);
   else
     fill_ones<float><<<1, 32, 0, ctx->stream>>>((float*)ctx->d_ones);
   CK(cudaGetLastError());
@@ -319,6 +338,7 @@ int tnsp_lattice_upload(tnsp_ctx* ctx, int L1, int L2, int P, const int* dims, c
     free_lattice(ctx);
     CK(cudaMalloc((void**)&ctx->dA64, sizeof(double) * total));
     CK(cudaMalloc((void**)&ctx->dA32, sizeof(float) * total));
+    CK(cudaMalloc((void**)&ctx->dAdd, sizeof(dd) * total));
     CK(cudaMalloc((void**)&ctx->d_dims, sizeof(int) * dv.size()));
     CK(cudaMalloc((void**)&ctx->d_off, sizeof(long long) * off.size()));
     CK(cudaMalloc((void**)&ctx->d_qleg, sizeof(int) * (size_t)L1 * L2 * 4 * Dmax));
@@ -330,9 +350,10 @@ int tnsp_lattice_upload(tnsp_ctx* ctx, int L1, int L2, int P, const int* dims, c
     ctx->charged = false;
   }
   ctx->hostA.assign(tensors, tensors + total);
-  std::vector<float> a32(tensors, tensors + total);
   CK(cudaMemcpyAsync(ctx->dA64, tensors, sizeof(double) * total, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->dA32, a32.data(), sizeof(float) * total, cudaMemcpyHostToDevice, ctx->stream));
+  convert_tensors<<<(int)std::min<long long>(1024, (total + 255) / 256), 256, 0, ctx->stream>>>(ctx->dA64, total,
+                                                                                               ctx->dA32, ctx->dAdd);
+  CK(cudaGetLastError());
   CK(cudaMemcpyAsync(ctx->d_dims, dv.data(), sizeof(int) * dv.size(), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->d_off, off.data(), sizeof(long long) * off.size(), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -433,6 +454,7 @@ int tnsp_model_upload(tnsp_ctx* ctx, int n_terms, const int* sites, const int* o
   }
   for (int e = 0; e < n_entries; ++e)
     if (out_index[e] < 0 || out_index[e] >= P * P) return fail(ctx, TNSP_E_ARG, "table output index out of range");
+  const bool terms_changed = !ctx->has_model || n_terms != ctx->n_terms;
   free_model(ctx);
   const size_t tp = (size_t)std::max(1, n_terms) * P * P;
   CK(cudaMalloc((void**)&ctx->d_term_sites, sizeof(int) * std::max(1, n_terms) * 4));
@@ -457,7 +479,7 @@ int tnsp_model_upload(tnsp_ctx* ctx, int n_terms, const int* sites, const int* o
   CK(cudaMemcpy(ctx->d_hflip, hflip.data(), sizeof(int) * hflip.size(), cudaMemcpyHostToDevice));
   ctx->n_terms = n_terms;
   ctx->has_model = true;
-  free_slots(ctx);  // the contribution buffer depends on n_terms
+  if (terms_changed) free_slots(ctx);  // the contribution buffer depends on n_terms
   return TNSP_OK;
 }
 
@@ -466,7 +488,8 @@ int tnsp_chains_init(tnsp_ctx* ctx, int B, const int32_t* configs, const uint64_
   if (!ctx) return TNSP_E_ARG;
   if (!ctx->has_lattice || !ctx->has_model) return fail(ctx, TNSP_E_STATE, "upload the lattice and the model first");
   if (B < 1) return fail(ctx, TNSP_E_ARG, "need at least one chain");
-  if (precision != TNSP_FP64 && precision != TNSP_FP32) return fail(ctx, TNSP_E_ARG, "unknown precision");
+  if (precision != TNSP_FP64 && precision != TNSP_FP32 && precision != TNSP_DD)
+    return fail(ctx, TNSP_E_ARG, "unknown precision");
   if (!configs || !seeds) return fail(ctx, TNSP_E_ARG, "null configs or seeds");
   const int ns = ctx->L1 * ctx->L2;
   for (long long i = 0; i < (long long)B * ns; ++i)
@@ -544,6 +567,9 @@ int tnsp_sweep(tnsp_ctx* ctx, int nsweeps, int observe) {
     if (ctx->precision == TNSP_FP64)
       launch_sweep_f64(grid, ctx->smem_bytes, ctx->stream, md, ch, ctx->slots, ctx->d_scratch, ctx->d_ones, nsweeps,
                        observe, 0);
+    else if (ctx->precision == TNSP_DD)
+      launch_sweep_dd(grid, ctx->smem_bytes, ctx->stream, md, ch, ctx->slots, ctx->d_scratch, ctx->d_ones, nsweeps,
+                      observe, 0);
     else
       launch_sweep_f32(grid, ctx->smem_bytes, ctx->stream, md, ch, ctx->slots, ctx->d_scratch, ctx->d_ones, nsweeps,
                        observe, 0);
@@ -648,6 +674,9 @@ int tnsp_amplitude(tnsp_ctx* ctx, int B, const int32_t* configs, double* mantiss
   if (ctx->precision == TNSP_FP64)
     launch_amplitude_f64(grid, ctx->smem_bytes, ctx->stream, md, ctx->slots, ctx->d_scratch, ctx->d_ones, B, dconf,
                          dm, de, ctx->d_status);
+  else if (ctx->precision == TNSP_DD)
+    launch_amplitude_dd(grid, ctx->smem_bytes, ctx->stream, md, ctx->slots, ctx->d_scratch, ctx->d_ones, B, dconf,
+                        dm, de, ctx->d_status);
   else
     launch_amplitude_f32(grid, ctx->smem_bytes, ctx->stream, md, ctx->slots, ctx->d_scratch, ctx->d_ones, B, dconf,
                          dm, de, ctx->d_status);

@@ -4,7 +4,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import TNSP_FP32, TNSP_FP64, ptr
+from ._lib import PRECISIONS, TNSP_DD, TNSP_FP32, TNSP_FP64, ptr
 
 LN2 = 0.6931471805599453
 
@@ -29,6 +29,7 @@ class Sampler:
         self.B = 0
         self.precision = TNSP_FP64
         self._uploaded_version = None
+        self._static_uploaded = False
         self.upload()
 
     def _check(self, code, what):
@@ -49,6 +50,8 @@ class Sampler:
 
     # ---------------------------------------------------------------------------------------
     def upload(self):
+        """Uploads the site tensors (and their charges, which the library checks them against); the
+        Hamiltonian tables, which a gradient step does not change, only on the first call."""
         lat = self.lattice
         dims = np.ascontiguousarray(lat.dims())
         flat = np.ascontiguousarray(lat.flat_tensors())
@@ -61,14 +64,19 @@ class Sampler:
             self._check(
                 self.lib.tnsp_lattice_charges(self.ctx, ptr(q, ctypes.c_int), ptr(qp, ctypes.c_int),
                                               ptr(fl, ctypes.c_int)), "tnsp_lattice_charges")
-        n, sites, offs, cnts, outs, vals = lat.term_arrays()
-        self._check(
-            self.lib.tnsp_model_upload(self.ctx, n, ptr(sites, ctypes.c_int), ptr(offs, ctypes.c_int),
-                                       ptr(cnts, ctypes.c_int), len(outs), ptr(outs, ctypes.c_int),
-                                       ptr(vals, ctypes.c_double)), "tnsp_model_upload")
+        if not self._static_uploaded:
+            n, sites, offs, cnts, outs, vals = lat.term_arrays()
+            self._check(
+                self.lib.tnsp_model_upload(self.ctx, n, ptr(sites, ctypes.c_int), ptr(offs, ctypes.c_int),
+                                           ptr(cnts, ctypes.c_int), len(outs), ptr(outs, ctypes.c_int),
+                                           ptr(vals, ctypes.c_double)), "tnsp_model_upload")
+            self._static_uploaded = True
         self._uploaded_version = lat.version
 
     def init_chains(self, configs, seeds, discard=0, precision=TNSP_FP64):
+        """``precision``: TNSP_FP64 / TNSP_FP32 / TNSP_DD or one of "fp64", "fp32", "dd"."""
+        if isinstance(precision, str):
+            precision = PRECISIONS[precision]
         configs = np.ascontiguousarray(configs, dtype=np.int32)
         seeds = np.ascontiguousarray(seeds, dtype=np.uint64)
         B = seeds.shape[0]

@@ -24,7 +24,7 @@ gradient, no configuration cache (``NotImplementedError`` where the reference wo
 import numpy as np
 
 from .engine import Sampler, estimators, gradient_from
-from ._lib import TNSP_FP32, TNSP_FP64
+from ._lib import PRECISIONS
 
 
 class Configuration:
@@ -86,7 +86,9 @@ class SweepSampling:
         if self.seeds.shape != (chains,):
             raise ValueError("one seed per chain")
         self.discard = discard
-        self.precision = TNSP_FP32 if precision == "fp32" else TNSP_FP64
+        if precision not in PRECISIONS:
+            raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
+        self.precision = PRECISIONS[precision]
         self._engine = Sampler(owner, cut_dimension, device=device)
         owner._gpu_engine = self._engine
         self._started = False
