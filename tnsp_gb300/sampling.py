@@ -27,6 +27,46 @@ from .engine import Sampler, estimators, gradient_from
 from ._lib import PRECISIONS
 
 
+def _process_group():
+    """(rank, world size, torch.distributed module) of the default process group, or (0, 1, None)."""
+    try:
+        import torch.distributed as dist
+    except ImportError:
+        return 0, 1, None
+    if not (dist.is_available() and dist.is_initialized()):
+        return 0, 1, None
+    return dist.get_rank(), dist.get_world_size(), dist
+
+
+def allreduce_sum(arrays):
+    """Sums float64 host arrays over the ranks of the default ``torch.distributed`` group, as the
+    reference's ``Observer.__exit__`` sums its accumulators with MPI Allreduce
+    (tetragono/tetragono/sampling_lattice/observer.py:89-126).  One collective for all arrays; the
+    identity without a group or with one rank."""
+    rank, world, dist = _process_group()
+    arrays = [np.asarray(a, dtype=np.float64) for a in arrays]
+    if world == 1:
+        return arrays
+    import torch
+    flat = torch.from_numpy(np.concatenate([a.ravel() for a in arrays]))
+    if dist.get_backend() == "nccl":
+        flat = flat.cuda()
+    dist.all_reduce(flat, op=dist.ReduceOp.SUM)
+    flat = flat.cpu().numpy()
+    out, o = [], 0
+    for a in arrays:
+        out.append(flat[o:o + a.size].reshape(a.shape))
+        o += a.size
+    return out
+
+
+def default_seeds(chains, seed_base=0):
+    """Chain b of rank r gets seed ``seed_base + r * chains + b``: distinct chains on every rank, as the
+    reference's SeedDiffer gives every MPI rank its own seed (tetragono/tetragono/utility.py:139-168)."""
+    rank, _, _ = _process_group()
+    return np.arange(chains, dtype=np.uint64) + np.uint64(seed_base + rank * chains)
+
+
 class Configuration:
     """One chain's configuration (``Configuration``, tetragono/tetragono/sampling_lattice/lattice.py:27-416),
     as seen by the driver: indexing and export/import of the int64 [L1, L2, orbit] array."""
@@ -70,7 +110,7 @@ class SweepSampling:
     (tetragono/tetragono/sampling_lattice/sampling.py:74-193) over ``chains`` GPU chains.
 
     ``seeds`` (one per chain) seed each chain's mt19937_64 as ``TAT.random.seed`` would; by default
-    chain b uses seed ``seed_base + b``.  ``discard`` skips that many uniform_real draws first (the
+    chain b uses seed ``seed_base + b`` (plus ``rank * chains`` under torch.distributed).  ``discard`` skips that many uniform_real draws first (the
     driver's ``SeedDiffer`` discards one)."""
 
     def __init__(self, owner, cut_dimension, restrict_subspace=None, hopping_hamiltonians=None, *, chains=1,
@@ -82,7 +122,7 @@ class SweepSampling:
         self.owner = owner
         self._cut_dimension = cut_dimension
         self.chains = chains
-        self.seeds = np.asarray(seeds if seeds is not None else np.arange(chains) + seed_base, dtype=np.uint64)
+        self.seeds = np.asarray(seeds if seeds is not None else default_seeds(chains, seed_base), dtype=np.uint64)
         if self.seeds.shape != (chains,):
             raise ValueError("one seed per chain")
         self.discard = discard
@@ -162,9 +202,16 @@ class Observer:
         if exc_type is not None:
             return False
         if self._engine is not None:
-            self._scalars, self._delta, self._edelta = self._engine.read_observer(
-                with_gradient=self._enable_gradient)
+            self._scalars, self._delta, self._edelta = self._reduced(
+                *self._engine.read_observer(with_gradient=self._enable_gradient))
         return False
+
+    def _reduced(self, scalars, delta, edelta):
+        """Sum over the ranks of a process group (one collective), as ``Observer.__exit__`` does."""
+        if delta is None:
+            scalars, = allreduce_sum([scalars])
+            return scalars, None, None
+        return tuple(allreduce_sum([scalars, delta, edelta]))
 
     def __call__(self, possibility, configuration):
         if not getattr(configuration, "_observed", False):
@@ -173,7 +220,8 @@ class Observer:
 
     def _read(self):
         if self._scalars is None:
-            self._scalars, self._delta, self._edelta = self._engine.read_observer(with_gradient=self._enable_gradient)
+            self._scalars, self._delta, self._edelta = self._reduced(
+                *self._engine.read_observer(with_gradient=self._enable_gradient))
         return self._scalars
 
     @property
