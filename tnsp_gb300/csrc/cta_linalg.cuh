@@ -67,6 +67,34 @@ __device__ __forceinline__ dd jacobi_tan(dd zeta) {
   return (zeta >= dd(0.f, 0.f) ? dd(1.f, 0.f) : dd(-1.f, 0.f)) / (fabs(zeta) + sqrt(dd(1.f, 0.f) + zeta * zeta));
 }
 
+// Plane rotation of one element pair: (u, v) -> (c u - s v, s u + c v).
+template <class T> __device__ __forceinline__ void rotate_pair(T c, T s, T& u, T& v) {
+  const T x = u, y = v;
+  u = c * x - s * y;
+  v = s * x + c * y;
+}
+__device__ __forceinline__ void rotate_pair(dd c, dd s, dd& u, dd& v) {
+  const dd x = u, y = v;
+  u = dd_lincomb(c, x, -s, y);
+  v = dd_lincomb(s, x, c, y);
+}
+
+// Rotates the element pairs (x[r], y[r]), r = lane, lane + 32, ... < n, two per step so that the
+// dependent chains of two elements interleave (the same arithmetic per element as one at a time).
+template <class T> __device__ __forceinline__ void rotate_vectors(T c, T s, T* x, T* y, int n, int lane) {
+  int r = lane;
+  for (; r + 32 < n; r += 64) {
+    T u0 = x[r], v0 = y[r], u1 = x[r + 32], v1 = y[r + 32];
+    rotate_pair(c, s, u0, v0);
+    rotate_pair(c, s, u1, v1);
+    x[r] = u0;
+    y[r] = v0;
+    x[r + 32] = u1;
+    y[r + 32] = v1;
+  }
+  if (r < n) rotate_pair(c, s, x[r], y[r]);
+}
+
 // Shared-memory accumulation of a threshold estimate (order-independent to rounding only).
 __device__ __forceinline__ void shared_accumulate(double* p, double v) { atomicAdd(p, v); }
 __device__ __forceinline__ void shared_accumulate(float* p, float v) { atomicAdd(p, v); }
@@ -279,18 +307,10 @@ __device__ int block_jacobi(int nv, int len, T* X, T* Vr, int max_sweeps) {
         const T t = jacobi_tan(zeta);
         const T c = (T)1 / sqrt((T)1 + t * t);
         const T s = c * t;
-        for (int r = lane; r < len; r += 32) {
-          const T u = xi[r], v = xj[r];
-          xi[r] = c * u - s * v;
-          xj[r] = s * u + c * v;
-        }
+        rotate_vectors(c, s, xi, xj, len, lane);
         T* vi = Vr + (long)i * nv;
         T* vj = Vr + (long)j * nv;
-        for (int r = lane; r < nv; r += 32) {
-          const T u = vi[r], v = vj[r];
-          vi[r] = c * u - s * v;
-          vj[r] = s * u + c * v;
-        }
+        rotate_vectors(c, s, vi, vj, nv, lane);
       }
       __syncthreads();
     }
@@ -505,19 +525,11 @@ __device__ int block_jacobi_multi(int ns, const int* nv, const int* len, T* cons
       const T tt = jacobi_tan(zeta);
       const T c = (T)1 / sqrt((T)1 + tt * tt);
       const T sn = c * tt;
-      for (int r = lane; r < L; r += 32) {
-        const T u = xi[r], v = xj[r];
-        xi[r] = c * u - sn * v;
-        xj[r] = sn * u + c * v;
-      }
+      rotate_vectors(c, sn, xi, xj, L, lane);
       const int n = nv[t];
       T* vi = Vs[t] + (long)i * n;
       T* vj = Vs[t] + (long)j * n;
-      for (int r = lane; r < n; r += 32) {
-        const T u = vi[r], v = vj[r];
-        vi[r] = c * u - sn * v;
-        vj[r] = sn * u + c * v;
-      }
+      rotate_vectors(c, sn, vi, vj, n, lane);
     }
     __syncthreads();
     // end of a sweep of some sets: converged or next sweep

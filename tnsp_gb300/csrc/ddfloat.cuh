@@ -5,8 +5,8 @@
 // (two-product, here with a fused multiply-add) followed by a renormalisation (fast two-sum); see
 // T. J. Dekker, "A floating-point technique for extending the available precision", Numer. Math. 18
 // (1971) 224-242, and D. E. Knuth, TAOCP vol. 2, 4.2.2.  Addition is the accurate variant (two-sum on
-// both components), also inside the fused multiply-add.  Division and square root take one Newton
-// correction of the float approximation.  The exponent range is that of float: the sampler keeps every tensor
+// both components); the multiply-add and the two-term linear combination two-sum the high parts and
+// renormalise once.  Division and square root take one Newton correction of the float approximation.  The exponent range is that of float: the sampler keeps every tensor
 // normalised to O(1) and carries magnitudes in separate integer exponents.
 #pragma once
 #include <cuda_runtime.h>
@@ -64,21 +64,30 @@ __device__ __forceinline__ dd& operator+=(dd& x, dd y) { return x = x + y; }
 __device__ __forceinline__ dd& operator-=(dd& x, dd y) { return x = x - y; }
 __device__ __forceinline__ dd& operator*=(dd& x, dd y) { return x = x * y; }
 
-// a * b + c: the product as (p, cross) (exact product of the high parts plus the cross terms), then
-// the accurate addition.  The cheaper form that two-sums only the high parts and renormalises once
-// loses accuracy in cancelling dot products: on rank-deficient matrices it let one-sided Jacobi mix
-// nearly degenerate singular vectors across the truncation (E_loc errors of 5e-4 against 2e-9 with
-// this form), so it is not used.
+// a * b + c: exact product of the high parts (p, its rounding error in the cross terms), two-sum with
+// c's high part, one renormalisation: 15 FP32 instructions.  Its error is bounded relative to the
+// operands (|a b| + |c|), as a float64 dot product's is relative to the sum of |terms|.
 __device__ __forceinline__ dd fma(dd a, dd b, dd c) {
   const float p = a.hi * b.hi;
   const float pe = fmaf(a.hi, b.hi, -p);
   const float cross = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, pe));
-  dd s = dd_two_sum(c.hi, p);
-  const dd t = dd_two_sum(c.lo, cross);
-  s.lo += t.hi;
-  s = dd_fast_two_sum(s.hi, s.lo);
-  s.lo += t.lo;
-  return dd_fast_two_sum(s.hi, s.lo);
+  const dd s = dd_two_sum(c.hi, p);
+  return dd_fast_two_sum(s.hi, s.lo + (c.lo + cross));
+}
+
+// a * x + b * y with one two-sum of the high products and one renormalisation (19 FP32 instructions
+// against 34 for two products and an addition): the Jacobi rotations
+__device__ __forceinline__ dd dd_lincomb(dd a, dd x, dd b, dd y) {
+  const float p1 = a.hi * x.hi;
+  const float e1 = fmaf(a.hi, x.hi, -p1);
+  const float p2 = b.hi * y.hi;
+  const float e2 = fmaf(b.hi, y.hi, -p2);
+  const dd h = dd_two_sum(p1, p2);
+  float t = fmaf(a.hi, x.lo, e1);
+  t = fmaf(a.lo, x.hi, t);
+  t = fmaf(b.hi, y.lo, t);
+  t = fmaf(b.lo, y.hi, t);
+  return dd_fast_two_sum(h.hi, h.lo + (t + e2));
 }
 
 __device__ __forceinline__ bool operator<(dd x, dd y) { return x.hi < y.hi || (x.hi == y.hi && x.lo < y.lo); }

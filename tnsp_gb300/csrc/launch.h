@@ -28,5 +28,8 @@ void launch_amplitude_dd(int grid, size_t smem, cudaStream_t st, const Model& md
 cudaError_t set_smem_limit_f64(int bytes);
 cudaError_t set_smem_limit_dd(int bytes);
 cudaError_t set_smem_limit_f32(int bytes);
+cudaError_t occupancy_f64(int smem_bytes, int* blocks_per_sm);
+cudaError_t occupancy_dd(int smem_bytes, int* blocks_per_sm);
+cudaError_t occupancy_f32(int smem_bytes, int* blocks_per_sm);
 
 }  // namespace tnsp

@@ -18,8 +18,18 @@ void launch_amplitude_dd(int grid, size_t smem, cudaStream_t st, const Model& md
 
 cudaError_t set_smem_limit_dd(int bytes) {
   cudaError_t e = cudaFuncSetAttribute(sweep_kernel<dd>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(amplitude_kernel<dd>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(sweep_kernel<dd>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(amplitude_kernel<dd>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(amplitude_kernel<dd>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+  return e;
+}
+
+cudaError_t occupancy_dd(int smem_bytes, int* blocks_per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sweep_kernel<dd>, kThreads, smem_bytes);
 }
 
 }  // namespace tnsp

@@ -18,8 +18,18 @@ void launch_amplitude_f32(int grid, size_t smem, cudaStream_t st, const Model& m
 
 cudaError_t set_smem_limit_f32(int bytes) {
   cudaError_t e = cudaFuncSetAttribute(sweep_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(amplitude_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(sweep_kernel<float>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(amplitude_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(amplitude_kernel<float>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+  return e;
+}
+
+cudaError_t occupancy_f32(int smem_bytes, int* blocks_per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sweep_kernel<float>, kThreads, smem_bytes);
 }
 
 }  // namespace tnsp

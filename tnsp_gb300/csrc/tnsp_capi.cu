@@ -171,8 +171,23 @@ int ensure_slots(tnsp_ctx* ctx) {
   Slots s{};
   plan_slots(ctx, s);
   ctx->elem = ctx->precision == TNSP_FP32 ? 4 : 8;
-  // as many resident blocks as fit: 3 per SM, bounded by a scratch budget of 64 GB
-  long long want = 3LL * sms;
+  // dynamic shared memory for sector staging.  Per block: 56 KB + ~15 KB static + 1 KB reserved, so
+  // three blocks fit in an SM's 228 KB (64 KB allowed only two); the register budget of the sweep
+  // kernel (168 per thread) also allows three 128-thread blocks.
+  ctx->smem_bytes = 56 * 1024;
+  int occ = 0;
+  if (ctx->precision == TNSP_FP64) {
+    CK(set_smem_limit_f64((int)ctx->smem_bytes));
+    CK(occupancy_f64((int)ctx->smem_bytes, &occ));
+  } else if (ctx->precision == TNSP_DD) {
+    CK(set_smem_limit_dd((int)ctx->smem_bytes));
+    CK(occupancy_dd((int)ctx->smem_bytes, &occ));
+  } else {
+    CK(set_smem_limit_f32((int)ctx->smem_bytes));
+    CK(occupancy_f32((int)ctx->smem_bytes, &occ));
+  }
+  // one resident wave of blocks (the occupancy limit per SM), bounded by a scratch budget of 64 GB
+  long long want = (long long)std::max(1, occ) * sms;
   const long long per = s.stride * (long long)ctx->elem + 2LL * ctx->n_params * 8;
   const long long budget = 64LL << 30;
   want = std::min(want, std::max(1LL, budget / std::max(1LL, per)));
@@ -196,15 +211,6 @@ int ensure_slots(tnsp_ctx* ctx) {
     CK(cudaMalloc((void**)&ctx->d_tfl, sizeof(int) * kMaxL * ctx->nslots));
     CK(cudaMalloc((void**)&ctx->d_ilist, sizeof(int) * (chi * ctx->Dmax + chi) * ctx->nslots));
   }
-  // dynamic shared memory for sector staging: 64 KB keeps three blocks per SM (the register
-  // budget of the sweep kernel allows three 128-thread blocks)
-  ctx->smem_bytes = 64 * 1024;
-  if (ctx->precision == TNSP_FP64)
-    CK(set_smem_limit_f64((int)ctx->smem_bytes));
-  else if (ctx->precision == TNSP_DD)
-    CK(set_smem_limit_dd((int)ctx->smem_bytes));
-  else
-    CK(set_smem_limit_f32((int)ctx->smem_bytes));
   CK(cudaMemsetAsync(ctx->d_flops, 0, sizeof(double) * kCounters * ctx->nslots, ctx->stream));
   CK(cudaMemsetAsync(ctx->d_delta, 0, sizeof(double) * ctx->n_params * ctx->nslots, ctx->stream));
   CK(cudaMemsetAsync(ctx->d_edelta, 0, sizeof(double) * ctx->n_params * ctx->nslots, ctx->stream));
