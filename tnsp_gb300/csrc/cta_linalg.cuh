@@ -95,6 +95,63 @@ template <class T> __device__ __forceinline__ void rotate_vectors(T c, T s, T* x
   if (r < n) rotate_pair(c, s, x[r], y[r]);
 }
 
+// Lane-group primitives of the Jacobi routines: a rotation pair is handled by a group of kJG lanes, so
+// a warp works on 32 / kJG pairs at once and the latency-bound parts of a pair step (the reductions
+// of its three dot products and the scalar angle computation) run for all of them in the same
+// instructions.
+constexpr int kJG = 8;
+__device__ __forceinline__ double shfl_xor(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ float shfl_xor(float v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+// Sum over the aligned group of G lanes (every lane of the warp must call it).
+template <int G, class T> __device__ __forceinline__ T group_sum(T v) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) v = v + shfl_xor(v, o);
+  return v;
+}
+// rotate_vectors for a G-lane group: elements r = sl, sl + G, ..., two per step
+template <int G, class T> __device__ __forceinline__ void rotate_group(T c, T s, T* x, T* y, int n, int sl) {
+  int r = sl;
+  for (; r + G < n; r += 2 * G) {
+    T u0 = x[r], v0 = y[r], u1 = x[r + G], v1 = y[r + G];
+    rotate_pair(c, s, u0, v0);
+    rotate_pair(c, s, u1, v1);
+    x[r] = u0;
+    y[r] = v0;
+    x[r + G] = u1;
+    y[r + G] = v1;
+  }
+  if (r < n) rotate_pair(c, s, x[r], y[r]);
+}
+// One pair step of one-sided Jacobi on vectors xi, xj (length len) with their accumulated rotations
+// vi, vj (length n), by a G-lane group (sub-lane sl).  Every lane of the warp calls it; groups without
+// a pair pass act = false (their pointers are not touched).  Returns true if the pair was rotated.
+// Pairs where either vector is below the noise floor, or that are orthogonal to tol, are left alone.
+template <int G, class T>
+__device__ __forceinline__ bool jacobi_pair(bool act, T* xi, T* xj, int len, T* vi, T* vj, int n, T noise2, T tol,
+                                            int sl) {
+  T a = 0, b = 0, g = 0;
+  if (act) {
+    for (int r = sl; r < len; r += G) {
+      const T u = xi[r], v = xj[r];
+      a = fma(u, u, a);
+      b = fma(v, v, b);
+      g = fma(u, v, g);
+    }
+  }
+  a = group_sum<G>(a);
+  b = group_sum<G>(b);
+  g = group_sum<G>(g);
+  if (!act || a <= noise2 || b <= noise2) return false;
+  if (!(fabs(g) > tol * sqrt(a) * sqrt(b))) return false;
+  const T zeta = (b - a) / ((T)2 * g);
+  const T t = jacobi_tan(zeta);
+  const T c = (T)1 / sqrt((T)1 + t * t);
+  const T s = c * t;
+  rotate_group<G>(c, s, xi, xj, len, sl);
+  rotate_group<G>(c, s, vi, vj, n, sl);
+  return true;
+}
+
 // Shared-memory accumulation of a threshold estimate (order-independent to rounding only).
 __device__ __forceinline__ void shared_accumulate(double* p, double v) { atomicAdd(p, v); }
 __device__ __forceinline__ void shared_accumulate(float* p, float v) { atomicAdd(p, v); }
@@ -174,88 +231,10 @@ __device__ void block_gemm(int m, int n, int k, const T* __restrict__ A, int lda
   __syncthreads();
 }
 
-// Householder QR of the row-major m x n matrix M (overwritten).  Writes Q (m x kk, row-major,
-// kk = min(m, n)) to Q and R (kk x n, row-major) to R.  tau: kk scratch values.
-// Reflector j: H_j = I - tau_j v v^T, v_j = 1, v below the diagonal stored in column j of M
-// (the LAPACK dgeqrf convention; any orthogonal gauge is acceptable to the callers).
-template <class T>
-__device__ void block_qr(int m, int n, T* M, T* Q, T* R, T* tau, T* red) {
-  const int kk = m < n ? m : n;
-  __shared__ T s_beta, s_tau, s_scale;
-  for (int j = 0; j < kk; ++j) {
-    // norm of M[j+1:m, j]
-    T part = 0;
-    for (int r = j + 1 + threadIdx.x; r < m; r += blockDim.x) {
-      const T x = M[(long)r * n + j];
-      part = fma(x, x, part);
-    }
-    const T sigma = block_sum(part, red);
-    if (threadIdx.x == 0) {
-      const T alpha = M[(long)j * n + j];
-      if (sigma == (T)0) {
-        s_tau = 0;
-        s_beta = alpha;
-        s_scale = 0;
-      } else {
-        T beta = sqrt(alpha * alpha + sigma);
-        if (alpha > 0) beta = -beta;
-        s_tau = (beta - alpha) / beta;
-        s_scale = (T)1 / (alpha - beta);
-        s_beta = beta;
-      }
-      tau[j] = s_tau;
-    }
-    __syncthreads();
-    const T tj = s_tau, sc = s_scale;
-    if (tj != (T)0) {
-      for (int r = j + 1 + threadIdx.x; r < m; r += blockDim.x) M[(long)r * n + j] *= sc;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) M[(long)j * n + j] = s_beta;
-    // apply H_j to columns j+1..n-1: warp per column
-    if (tj != (T)0) {
-      const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-      for (int c = j + 1 + w; c < n; c += kWarps) {
-        T d = lane == 0 ? M[(long)j * n + c] : (T)0;
-        for (int r = j + 1 + lane; r < m; r += 32) d = fma(M[(long)r * n + j], M[(long)r * n + c], d);
-        d = warp_sum(d) * tj;
-        if (lane == 0) M[(long)j * n + c] -= d;
-        for (int r = j + 1 + lane; r < m; r += 32) M[(long)r * n + c] -= d * M[(long)r * n + j];
-      }
-    }
-    __syncthreads();
-  }
-  // R = upper triangle of the first kk rows
-  for (long t = threadIdx.x; t < (long)kk * n; t += blockDim.x) {
-    const int i = (int)(t / n), c = (int)(t % n);
-    R[t] = c >= i ? M[(long)i * n + c] : (T)0;
-  }
-  // Q = H_0 ... H_{kk-1} [I; 0], accumulated backwards
-  for (long t = threadIdx.x; t < (long)m * kk; t += blockDim.x) {
-    const int i = (int)(t / kk), c = (int)(t % kk);
-    Q[t] = i == c ? (T)1 : (T)0;
-  }
-  __syncthreads();
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int j = kk - 1; j >= 0; --j) {
-    const T tj = tau[j];
-    if (tj != (T)0) {
-      for (int c = j + w; c < kk; c += kWarps) {
-        T d = lane == 0 ? Q[(long)j * kk + c] : (T)0;
-        for (int r = j + 1 + lane; r < m; r += 32) d = fma(M[(long)r * n + j], Q[(long)r * kk + c], d);
-        d = warp_sum(d) * tj;
-        if (lane == 0) Q[(long)j * kk + c] -= d;
-        for (int r = j + 1 + lane; r < m; r += 32) Q[(long)r * kk + c] -= d * M[(long)r * n + j];
-      }
-    }
-    __syncthreads();
-  }
-}
-
 // One-sided (Hestenes) Jacobi on nv vectors X[j][0..len) (vector-major), accumulating the same
 // rotations into Vr[j][0..nv) (initialised to the identity here).  Pairs are visited in the
-// round-robin (circle) order, one warp per pair.  Returns the number of sweeps, or -1 if the
-// sweep limit was reached without convergence.
+// round-robin (circle) order, one kJG-lane group per pair.  Returns the number of sweeps, or -1 if
+// the sweep limit was reached without convergence.
 template <class T>
 __device__ int block_jacobi(int nv, int len, T* X, T* Vr, int max_sweeps) {
   __shared__ int s_rot;
@@ -283,34 +262,21 @@ __device__ int block_jacobi(int nv, int len, T* X, T* Vr, int max_sweeps) {
     if (threadIdx.x == 0) s_rot = 0;
     __syncthreads();
     int rot = 0;
+    const int grp = lane / kJG, sl = lane % kJG;
     for (int round = 0; round < np - 1; ++round) {
-      for (int k = w; k < np / 2; k += kWarps) {
-        const int i = k == 0 ? 0 : ((k + round - 1) % (np - 1)) + 1;
-        const int j = ((np - 1 - k + round - 1) % (np - 1)) + 1;
-        if (i >= nv || j >= nv) continue;
-        T* xi = X + (long)i * len;
-        T* xj = X + (long)j * len;
-        T a = 0, b = 0, g = 0;
-        for (int r = lane; r < len; r += 32) {
-          const T u = xi[r], v = xj[r];
-          a = fma(u, u, a);
-          b = fma(v, v, b);
-          g = fma(u, v, g);
+      for (int base = w * (32 / kJG); base < np / 2; base += kWarps * (32 / kJG)) {  // warp-uniform
+        const int k = base + grp;
+        int i = 0, j = 0;
+        bool act = k < np / 2;
+        if (act) {
+          i = k == 0 ? 0 : ((k + round - 1) % (np - 1)) + 1;
+          j = ((np - 1 - k + round - 1) % (np - 1)) + 1;
+          act = i < nv && j < nv;
         }
-        a = warp_sum(a);
-        b = warp_sum(b);
-        g = warp_sum(g);
-        if (a <= noise2 || b <= noise2) continue;
-        if (!(fabs(g) > tol * sqrt(a) * sqrt(b))) continue;
-        rot = 1;
-        const T zeta = (b - a) / ((T)2 * g);
-        const T t = jacobi_tan(zeta);
-        const T c = (T)1 / sqrt((T)1 + t * t);
-        const T s = c * t;
-        rotate_vectors(c, s, xi, xj, len, lane);
-        T* vi = Vr + (long)i * nv;
-        T* vj = Vr + (long)j * nv;
-        rotate_vectors(c, s, vi, vj, nv, lane);
+        if (!act) i = j = 0;
+        if (jacobi_pair<kJG>(act, X + (long)i * len, X + (long)j * len, len, Vr + (long)i * nv, Vr + (long)j * nv, nv,
+                             noise2, tol, sl))
+          rot = 1;
       }
       __syncthreads();
     }
@@ -373,11 +339,33 @@ template <class Pred> __device__ int block_compact(int n, Pred pred, int* out, i
 // ---------------------------------------------------------------------------------------------
 // column-major Householder QR (LAPACK geqr2 / org2r conventions, any orthogonal gauge is fine)
 // ---------------------------------------------------------------------------------------------
+// Applies the reflector H = I - tau v v^T to columns c0..n-1 of the column-major m-row matrix G, one
+// kJG-lane group per column.  v occupies rows r0..m-1 of column-major storage `v`; with unit_head
+// its row-r0 entry is an implicit 1 (geqrf layout: R's diagonal sits there), else it is stored.
+template <class T>
+__device__ __forceinline__ void apply_reflector_cm(int m, int r0, const T* v, bool unit_head, T tau, T* G, int c0,
+                                                   int n) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, grp = lane / kJG, sl = lane % kJG;
+  const int rs = unit_head ? r0 + 1 : r0;
+  for (int base = c0 + w * (32 / kJG); base < n; base += kWarps * (32 / kJG)) {  // warp-uniform
+    const int c = base + grp;
+    const bool act = c < n;
+    T* gc = G + (long)(act ? c : base) * m;
+    T d = (act && unit_head && sl == 0) ? gc[r0] : (T)0;
+    if (act)
+      for (int r = rs + sl; r < m; r += kJG) d = fma(v[r], gc[r], d);
+    d = group_sum<kJG>(d) * tau;
+    if (act) {
+      if (unit_head && sl == 0) gc[r0] -= d;
+      for (int r = rs + sl; r < m; r += kJG) gc[r] -= d * v[r];
+    }
+  }
+}
+
 // G: m x n column-major (ld = m), overwritten by R (upper triangle) and the reflectors below it.
 template <class T> __device__ void block_geqrf_cm(int m, int n, T* G, T* tau, T* red) {
   const int kk = m < n ? m : n;
   __shared__ T s_beta, s_tau, s_scale;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int j = 0; j < kk; ++j) {
     T* gj = G + (long)j * m;
     T part = 0;
@@ -404,38 +392,20 @@ template <class T> __device__ void block_geqrf_cm(int m, int n, T* G, T* tau, T*
       for (int r = j + 1 + threadIdx.x; r < m; r += blockDim.x) gj[r] *= sc;
     __syncthreads();
     if (threadIdx.x == 0) gj[j] = s_beta;
-    if (tj != (T)0) {
-      for (int c = j + 1 + w; c < n; c += kWarps) {
-        T* gc = G + (long)c * m;
-        T d = lane == 0 ? gc[j] : (T)0;
-        for (int r = j + 1 + lane; r < m; r += 32) d = fma(gj[r], gc[r], d);
-        d = warp_sum(d) * tj;
-        if (lane == 0) gc[j] -= d;
-        for (int r = j + 1 + lane; r < m; r += 32) gc[r] -= d * gj[r];
-      }
-    }
+    if (tj != (T)0) apply_reflector_cm(m, j, gj, true, tj, G, j + 1, n);
     __syncthreads();
   }
 }
 
 // Forms Q (m x k, first k columns of G, column-major) in place from block_geqrf_cm's reflectors.
 template <class T> __device__ void block_orgqr_cm(int m, int k, T* G, const T* tau) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int i = k - 1; i >= 0; --i) {
     T* gi = G + (long)i * m;
     const T ti = tau[i];
     if (i < k - 1) {
       if (threadIdx.x == 0) gi[i] = (T)1;
       __syncthreads();
-      if (ti != (T)0) {
-        for (int c = i + 1 + w; c < k; c += kWarps) {
-          T* gc = G + (long)c * m;
-          T d = 0;
-          for (int r = i + lane; r < m; r += 32) d = fma(gi[r], gc[r], d);
-          d = warp_sum(d) * ti;
-          for (int r = i + lane; r < m; r += 32) gc[r] -= d * gi[r];
-        }
-      }
+      if (ti != (T)0) apply_reflector_cm(m, i, gi, false, ti, G, i + 1, k);
       __syncthreads();
     }
     for (int r = i + 1 + threadIdx.x; r < m; r += blockDim.x) gi[r] *= -ti;
@@ -455,7 +425,7 @@ template <class T> __device__ void block_orgqr_cm(int m, int k, T* G, const T* t
 // circle ordering and convergence test (rotation rule and tolerance of block_jacobi, noise floor
 // tol^2 * |A|_F^2), but all sets advance together: a block barrier ends one round of every set, so
 // the number of barriers is set by the largest set instead of the sum over sets.  Pairs of a round
-// are spread over the warps.  Returns the largest sweep count, or -1 if a set hit max_sweeps.
+// are spread over kJG-lane groups of all warps.  Returns the largest sweep count, or -1 if a set hit max_sweeps.
 template <class T, int MAXS>
 __device__ int block_jacobi_multi(int ns, const int* nv, const int* len, T* const* Xs, T* const* Vs, int max_sweeps) {
   __shared__ int s_np[MAXS], s_pp[MAXS + 1], s_rot[MAXS], s_done[MAXS], s_sweeps[MAXS];
@@ -493,43 +463,32 @@ __device__ int block_jacobi_multi(int ns, const int* nv, const int* len, T* cons
   }
   __syncthreads();
   for (int g = 0;; ++g) {
-    // pairs of round g of every unfinished set
+    // pairs of round g of every unfinished set, one kJG-lane group per pair
     const int total = s_pp[ns];
-    for (int p = w; p < total; p += kWarps) {
-      int t = 0;
-      while (p >= s_pp[t + 1]) ++t;
-      if (s_done[t]) continue;
-      const int np = s_np[t], k = p - s_pp[t], rounds = np - 1;
-      const int round = g % rounds;
-      const int i = k == 0 ? 0 : ((k + round - 1) % rounds) + 1;
-      const int j = ((np - 1 - k + round - 1) % rounds) + 1;
-      if (i >= nv[t] || j >= nv[t]) continue;
-      const int L = len[t];
-      T* xi = Xs[t] + (long)i * L;
-      T* xj = Xs[t] + (long)j * L;
-      T a = 0, b = 0, c2 = 0;
-      for (int r = lane; r < L; r += 32) {
-        const T u = xi[r], v = xj[r];
-        a = fma(u, u, a);
-        b = fma(v, v, b);
-        c2 = fma(u, v, c2);
+    const int grp = lane / kJG, sl = lane % kJG;
+    for (int base = w * (32 / kJG); base < total; base += kWarps * (32 / kJG)) {  // warp-uniform
+      const int p = base + grp;
+      bool act = p < total;
+      int t = 0, i = 0, j = 0;
+      if (act) {
+        while (p >= s_pp[t + 1]) ++t;
+        act = !s_done[t];
       }
-      a = warp_sum(a);
-      b = warp_sum(b);
-      c2 = warp_sum(c2);
+      if (act) {
+        const int np = s_np[t], k = p - s_pp[t], rounds = np - 1;
+        const int round = g % rounds;
+        i = k == 0 ? 0 : ((k + round - 1) % rounds) + 1;
+        j = ((np - 1 - k + round - 1) % rounds) + 1;
+        act = i < nv[t] && j < nv[t];
+      }
+      const int L = act ? len[t] : 0, n = act ? nv[t] : 0;
+      T* xi = act ? Xs[t] + (long)i * L : nullptr;
+      T* xj = act ? Xs[t] + (long)j * L : nullptr;
+      T* vi = act ? Vs[t] + (long)i * n : nullptr;
+      T* vj = act ? Vs[t] + (long)j * n : nullptr;
       const T tol = Eps<T>::value() * (T)(L > 32 ? L : 32);
-      if (a <= s_noise[t] || b <= s_noise[t]) continue;
-      if (!(fabs(c2) > tol * sqrt(a) * sqrt(b))) continue;
-      if (lane == 0) s_rot[t] = 1;
-      const T zeta = (b - a) / ((T)2 * c2);
-      const T tt = jacobi_tan(zeta);
-      const T c = (T)1 / sqrt((T)1 + tt * tt);
-      const T sn = c * tt;
-      rotate_vectors(c, sn, xi, xj, L, lane);
-      const int n = nv[t];
-      T* vi = Vs[t] + (long)i * n;
-      T* vj = Vs[t] + (long)j * n;
-      rotate_vectors(c, sn, vi, vj, n, lane);
+      const T noise = act ? s_noise[t] : (T)0;
+      if (jacobi_pair<kJG>(act, xi, xj, L, vi, vj, n, noise, tol, sl) && sl == 0) s_rot[t] = 1;
     }
     __syncthreads();
     // end of a sweep of some sets: converged or next sweep
@@ -653,16 +612,7 @@ template <class T> __device__ void block_geqp3_cm(int m, int n, T* G, T* tau, in
       for (int r = j + 1 + threadIdx.x; r < m; r += blockDim.x) gj[r] *= sc;
     __syncthreads();
     if (threadIdx.x == 0) gj[j] = s_beta;
-    if (tj != (T)0) {
-      for (int c = j + 1 + w; c < n; c += kWarps) {
-        T* gc = G + (long)c * m;
-        T d = lane == 0 ? gc[j] : (T)0;
-        for (int r = j + 1 + lane; r < m; r += 32) d = fma(gj[r], gc[r], d);
-        d = warp_sum(d) * tj;
-        if (lane == 0) gc[j] -= d;
-        for (int r = j + 1 + lane; r < m; r += 32) gc[r] -= d * gj[r];
-      }
-    }
+    if (tj != (T)0) apply_reflector_cm(m, j, gj, true, tj, G, j + 1, n);
     __syncthreads();
   }
 }

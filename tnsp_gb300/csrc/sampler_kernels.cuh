@@ -1343,7 +1343,7 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Sl
       double ws_m;
       int ws_e;
       eng.hole0(ws_m, ws_e);
-      __shared__ double s_rw, s_ws;
+      __shared__ double s_rw;
       if (threadIdx.x == 0) {
         const double r = ratio_of(ws_m, ws_e, s_ws_m, s_ws_e);  // ws / ws_sweep
         s_rw = r * r;                                          // |ws|^2 / possibility
