@@ -100,3 +100,21 @@ def test_site_charges_conserve_on_reference_tensors(name):
             t = g.z[f"site_{l1}_{l2}_dense"]
             for p, u, d, l, r in np.argwhere(t != 0):
                 assert phys[p] + legs["U"][u] + legs["D"][d] + legs["L"][l] + legs["R"][r] == flux
+
+
+def test_precision_names_match_the_header():
+    """Python precision names map to the header's TNSP_FP64 / TNSP_FP32 / TNSP_DD values."""
+    from tnsp_gb300._lib import PRECISIONS
+    header = open(os.path.join(ROOT, "include", "tnsp_gb300.h")).read()
+    values = {k: int(v) for k, v in re.findall(r"#define (TNSP_(?:FP64|FP32|DD)) (\d+)", header)}
+    assert PRECISIONS == {"fp64": values["TNSP_FP64"], "fp32": values["TNSP_FP32"], "dd": values["TNSP_DD"]}
+
+
+def test_sweep_sampling_rejects_unknown_precision_before_the_device():
+    from tnsp_gb300.lattice import random_heisenberg
+    from tnsp_gb300.sampling import SweepSampling
+    lat = random_heisenberg(2, 2, 2, seed=1)
+    with pytest.raises(ValueError):
+        SweepSampling(lat, 4, precision="fp16")
+    with pytest.raises(NotImplementedError):
+        SweepSampling(lat, 4, restrict_subspace=lambda c: True)
