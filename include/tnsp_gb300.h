@@ -126,6 +126,21 @@ int tnsp_observer_read(tnsp_ctx* ctx, double* scalars, double* delta, double* ed
  */
 int tnsp_samples_read(tnsp_ctx* ctx, double* eloc, double* log_ws, double* reweight);
 
+/*
+ * Natural gradient support.  tnsp_holes_keep(ctx, 1) makes every observed sweep append, per sample,
+ * the row <psi|s|dpsi/dA>/<psi|s|psi> over all parameters (dense A[p][u][d][l][r] order of the
+ * upload, zero outside the sampled physical slices; row order: sweep-major, then chain, following
+ * tnsp_samples_read) until the next tnsp_observer_reset; 0 releases the rows.  tnsp_holes_count gives
+ * the number of rows kept.  tnsp_holes_gemv computes y = H x (transpose == 0: x has n_params
+ * entries, y one per row) or y = H^T x (transpose != 0) on the device, x and y in host memory.
+ * Replaces: the per-sample deltas Observer.__call__ keeps with enable_natural_gradient
+ * (tetragono/tetragono/sampling_lattice/observer.py:403-409) and the D / DT products of
+ * natural_gradient_by_conjugate_gradient (observer.py:612-641).
+ */
+int tnsp_holes_keep(tnsp_ctx* ctx, int enable);
+int tnsp_holes_count(tnsp_ctx* ctx, int64_t* rows);
+int tnsp_holes_gemv(tnsp_ctx* ctx, int transpose, const double* x, double* y);
+
 /* Copies the chains' current configurations (export_configuration, lattice.py:208-229) and, if
  * not NULL, the sampling weight log|ws|^2 of their last sweep (log of `possibility`). */
 int tnsp_chains_read(tnsp_ctx* ctx, int32_t* configs, double* log_possibility);

@@ -491,8 +491,10 @@ def observe(peps, conf, env=None):
 class ObserverAccumulator:
     """The energy/gradient accumulators of ``Observer`` (observer.py:41-126, 313-415)."""
 
-    def __init__(self, peps):
+    def __init__(self, peps, natural=False):
         self.peps = peps
+        # per-sample (reweight, E_loc, dense hole row) kept for the natural gradient (observer.py:403-409)
+        self.samples = [] if natural else None
         self.count = 0
         self.total_weight = 0.0
         self.total_weight_square = 0.0
@@ -521,6 +523,14 @@ class ObserverAccumulator:
                 s = conf[l1, l2]
                 self.Delta[l1][l2][s] += h
                 self.EDelta[l1][l2][s] += eloc * h
+        if self.samples is not None:
+            row = []
+            for l1 in range(self.peps.L1):
+                for l2 in range(self.peps.L2):
+                    full = np.zeros_like(self.peps.A[l1][l2])
+                    full[conf[l1, l2]] = holes[l1][l2]
+                    row.append(full.ravel())
+            self.samples.append((reweight, eloc, np.concatenate(row)))
         return ws, eloc, holes
 
     def total_energy(self):
@@ -535,6 +545,56 @@ class ObserverAccumulator:
     def energy(self):
         e, d = self.total_energy()
         return e / self.peps.site_number, d / self.peps.site_number
+
+    def natural_gradient(self, step, error):
+        """``Observer.natural_gradient_by_conjugate_gradient`` (observer.py:576-675) for real tensors:
+        conjugate gradient on D^T D x = D^T E with D_s = (delta_s - <delta>) sqrt(w_s / W) and
+        E_s = (E_loc,s - <E>) sqrt(w_s / W), stopped after `step` steps or when |r|^2 / |b|^2 < error^2;
+        returns 2 x per site.  Rows are dense (P, U, D, L, R) per site, concatenated in site order."""
+        W = self.total_weight
+        energy = self.er / W
+        delta = np.concatenate([d.ravel() for row in self.Delta for d in row]) / W
+        param = np.array([(r / W)**0.5 for r, _, _ in self.samples])
+        Dm = np.array([(h - delta) * c for (_, _, h), c in zip(self.samples, param)])
+        En = np.array([(e - energy) * c for (_, e, _), c in zip(self.samples, param)])
+
+        def D(v):
+            return Dm @ v
+
+        def DT(v):
+            return Dm.T @ v
+
+        b = DT(En)
+        b_square = np.dot(b, b)
+        x = np.zeros_like(b)
+        r = b - DT(D(x))
+        p = r
+        r_square = np.dot(r, r)
+        t = 0
+        while True:
+            if t == step:
+                break
+            if error != 0.0 and error**2 > r_square / b_square:
+                break
+            Dp = D(p)
+            alpha = r_square / np.dot(Dp, Dp)
+            x = x + alpha * p
+            r = r - alpha * DT(Dp)
+            new_r_square = np.dot(r, r)
+            beta = new_r_square / r_square
+            r_square = new_r_square
+            p = r + beta * p
+            t += 1
+        x = 2 * x
+        out, o = [], 0
+        for l1 in range(self.peps.L1):
+            row = []
+            for l2 in range(self.peps.L2):
+                n = self.peps.A[l1][l2].size
+                row.append(x[o:o + n].reshape(self.peps.A[l1][l2].shape))
+                o += n
+            out.append(row)
+        return out, t
 
     def gradient(self):
         """``Observer.gradient`` (observer.py:542-555) for real tensors."""

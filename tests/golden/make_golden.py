@@ -28,7 +28,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+_ARGS = [a for a in sys.argv[1:] if not a.startswith("--")]
+REF = _ARGS[0] if _ARGS else "/root/reference"
 
 
 def install_mpi_stub():
@@ -251,6 +252,38 @@ def run_case(name, kind, L1, L2, D, cut, tensor_seed, chain_seeds, n_therm, n_sa
     print(f"{name}: E/site = {energy:.12f} +- {error:.3e}, saved {os.path.getsize(path)} bytes")
 
 
+def run_natural_case(name, kind, L1, L2, D, cut, tensor_seed, chain_seeds, n_therm, n_samples, runs):
+    """The chains of case `name` again, observed with enable_natural_gradient; saves the reference's
+    natural_gradient_by_conjugate_gradient(step, error) (observer.py:576-675) for every (step, error)
+    in `runs` to <name>_natgrad.npz."""
+    lattice = build_lattice(kind, L1, L2, D, tensor_seed)
+    neel = np.zeros((L1, L2, 1), dtype=np.int64)
+    for l1 in range(L1):
+        for l2 in range(L2):
+            neel[l1, l2, 0] = (l1 + l2) % 2
+    out = {"runs": np.array(runs, dtype=np.float64)}
+    # the reference releases its per-sample deltas after one natural-gradient call: one observed run
+    # of the (deterministic) chains per (step, error) setting
+    for k, (steps, error) in enumerate(runs):
+        observer = tet.Observer(lattice, enable_energy=True, enable_gradient=True, enable_natural_gradient=True)
+        with observer:
+            for seed in chain_seeds:
+                TAT.random.seed(seed)
+                sampling = tet.SweepSampling(lattice, cut, None, None)
+                sampling.configuration.import_configuration(neel)
+                for step in range(n_therm + n_samples):
+                    possibility, configuration = sampling()
+                    if step >= n_therm:
+                        observer(possibility, configuration)
+        grad = observer.natural_gradient_by_conjugate_gradient(int(steps), float(error))
+        for l1 in range(L1):
+            for l2 in range(L2):
+                out[f"natgrad{k}_{l1}_{l2}"] = dense_site(grad[l1][l2])
+    path = os.path.join(HERE, f"{name}_natgrad.npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: natural gradient for {len(runs)} (step, error) settings, saved {os.path.getsize(path)} bytes")
+
+
 def _same_shapes(holes, L1, L2):
     return False
 
@@ -259,9 +292,12 @@ def _pack_holes(holes, L1, L2):
     return [[dense_site(holes[l1][l2]) for l2 in range(L2)] for l1 in range(L1)]
 
 
-if __name__ == "__main__":
+if __name__ == "__main__" and "--natural-only" not in sys.argv:
     run_case("heis_no_3x3_D3_dc4", "no", 3, 3, 3, 4, 1234, [11, 12], 3, 5)
     run_case("heis_no_4x4_D4_dc16", "no", 4, 4, 4, 16, 2024, [21, 22], 4, 6)
     run_case("heis_no_4x4_D3_dc5", "no", 4, 4, 3, 5, 77, [31], 3, 5)
     run_case("heis_u1_4x4_D111_dc5", "u1", 4, 4, (1, 1, 1), 5, 4321, [41, 42], 3, 5)
     run_case("heis_u1_4x4_D222_dc8", "u1", 4, 4, (2, 2, 2), 8, 8765, [51], 2, 4)
+if __name__ == "__main__":
+    run_natural_case("heis_no_3x3_D3_dc4", "no", 3, 3, 3, 4, 1234, [11, 12], 3, 5, [(6, 0.0), (50, 1e-3)])
+    run_natural_case("heis_u1_4x4_D111_dc5", "u1", 4, 4, (1, 1, 1), 5, 4321, [41, 42], 3, 5, [(6, 0.0), (50, 1e-3)])

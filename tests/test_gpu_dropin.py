@@ -43,3 +43,35 @@ def test_driver_loop_matches_reference(name):
     state.apply_gradient(grad, 0.01)
     observer.normalize_lattice()
     assert state.lattice_dot() != norm0
+
+
+@pytest.mark.parametrize("name", ["heis_no_3x3_D3_dc4", "heis_u1_4x4_D111_dc5"])
+def test_natural_gradient_matches_reference(name):
+    """Observer(enable_natural_gradient=True) + natural_gradient_by_conjugate_gradient(step, error)
+    against the reference's own outputs (fixed step count, and error-based stop)."""
+    import os
+    from golden_cases import GOLDEN
+    from test_gpu_parity import make_lattice
+    from tnsp_gb300.sampling import Observer, SweepSampling
+    g = Golden(name)
+    nat = np.load(os.path.join(GOLDEN, f"{name}_natgrad.npz"))
+    state = make_lattice(g, charged=True)
+    seeds = g.meta["chain_seeds"]
+    chains = len(seeds)
+    nt, ns = g.meta["n_therm"], g.meta["n_samples"]
+    sampling = SweepSampling(state, g.cut, None, None, chains=chains, seeds=seeds)
+    sampling.configuration.import_configuration(g.neel()[:, :, None])
+    for _ in range(nt * chains):
+        sampling()
+    observer = Observer(state, enable_energy=True, enable_gradient=True, enable_natural_gradient=True)
+    with observer:
+        for _ in range(ns * chains):
+            possibility, configuration = sampling()
+            observer(possibility, configuration)
+    for k, (steps, error) in enumerate(nat["runs"]):
+        grad = observer.natural_gradient_by_conjugate_gradient(int(steps), float(error))
+        scale = max(np.abs(nat[f"natgrad{k}_{l1}_{l2}"]).max() for l1 in range(g.L1) for l2 in range(g.L2))
+        for l1 in range(g.L1):
+            for l2 in range(g.L2):
+                ref = nat[f"natgrad{k}_{l1}_{l2}"]
+                assert np.abs(grad[l1][l2] - ref).max() <= 1e-8 * scale, (k, l1, l2)

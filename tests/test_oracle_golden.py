@@ -1,8 +1,9 @@
 """The oracle (CPU restatement) against the reference's own outputs (tests/golden/)."""
+import os
 import numpy as np
 import pytest
 
-from golden_cases import CASES, Golden
+from golden_cases import CASES, GOLDEN, Golden
 from oracle.peps_oracle import DensePEPS, ObserverAccumulator, SweepChain, sweep_order
 from oracle.rng import MT19937_64, uniform_int, uniform_real01
 
@@ -74,3 +75,29 @@ def test_oracle_matches_reference(name, charged):
         for l2 in range(g.L2):
             ref = z[f"grad_{l1}_{l2}"]
             assert np.abs(grad[l1][l2] - ref).max() <= 1e-10 * max(1.0, np.abs(ref).max())
+
+
+NATURAL_CASES = ["heis_no_3x3_D3_dc4", "heis_u1_4x4_D111_dc5"]
+
+
+@pytest.mark.parametrize("name", NATURAL_CASES)
+def test_oracle_natural_gradient_matches_reference(name):
+    """Conjugate-gradient natural gradient of the oracle against the reference's own
+    natural_gradient_by_conjugate_gradient (observer.py:576-675), fixed step count and error stop."""
+    g = Golden(name)
+    nat = np.load(os.path.join(GOLDEN, f"{name}_natgrad.npz"))
+    peps = DensePEPS(g.dense_sites(), g.terms(), g.cut)
+    acc = ObserverAccumulator(peps, natural=True)
+    for seed in g.meta["chain_seeds"]:
+        chain = SweepChain(peps, g.neel(), seed)
+        for k in range(g.meta["n_therm"] + g.meta["n_samples"]):
+            poss, conf = chain.sweep()
+            if k >= g.meta["n_therm"]:
+                acc.add(poss, conf, chain.env)
+    for k, (steps, error) in enumerate(nat["runs"]):
+        grad, _ = acc.natural_gradient(int(steps), float(error))
+        scale = max(np.abs(nat[f"natgrad{k}_{l1}_{l2}"]).max() for l1 in range(g.L1) for l2 in range(g.L2))
+        for l1 in range(g.L1):
+            for l2 in range(g.L2):
+                ref = nat[f"natgrad{k}_{l1}_{l2}"]
+                assert np.abs(grad[l1][l2] - ref).max() <= 1e-8 * scale, (k, l1, l2)

@@ -51,6 +51,12 @@ struct tnsp_ctx {
   int32_t* d_status = nullptr;
   double* d_rec = nullptr;  // 3 x rec_cap x B
   int rec_cap = 0, rec_n = 0;
+  // per-sample hole rows kept for the natural gradient (tnsp_holes_keep): holes_rows x n_params
+  bool keep_holes = false;
+  double* d_holes = nullptr;
+  long long holes_rows = 0, holes_cap = 0;
+  double* d_gemv = nullptr;  // operand / result staging of tnsp_holes_gemv
+  long long gemv_cap = 0;
   // slots
   int nslots = 0;
   tnsp::Slots slots{};

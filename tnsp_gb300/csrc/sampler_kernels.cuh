@@ -74,6 +74,11 @@ struct Chains {
   double* rec_logws;
   double* rec_rw;
   int32_t* status;
+  // optional per-sample hole rows for the natural gradient: row hole_row0 + sweep * B + chain holds
+  // <psi|s|d psi / d A> / <psi|s|psi> for every parameter (zero outside the sampled physical slices;
+  // the rows are zeroed before the launch)
+  double* rec_hole;
+  long long hole_row0;
 };
 
 struct Slots {
@@ -1420,7 +1425,8 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Sl
                                   (double)ud.p * dd.p * ed.p * fd.p * ud.b * dd.b));
             }
             const int ex = s_eE[l2] + s_eF[l2 + 1] + eng.lexpo(F_UP, l1 - 1) + eng.lexpo(F_DOWN, l1 + 1);
-            const double f = ldexp(1.0 / ws_m, ex - ws_e) * rw;
+            const double fh = ldexp(1.0 / ws_m, ex - ws_e);  // hole / ws
+            const double f = fh * rw;
             const int id = l1 * md.L2 + l2;
             const int* d = md.dims + id * 4;
             const long long n = (long long)d[0] * d[1] * d[2] * d[3];
@@ -1429,6 +1435,10 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Sl
               const double hv = (double)h[q] * f;
               delta[base + q] += hv;
               edelta[base + q] += eloc * hv;
+            }
+            if (ch.rec_hole) {
+              double* row = ch.rec_hole + (ch.hole_row0 + (long long)(rec_base + sw) * ch.B + b) * md.n_params;
+              for (long long q = threadIdx.x; q < n; q += blockDim.x) row[base + q] = (double)h[q] * fh;
             }
             __syncthreads();
           }

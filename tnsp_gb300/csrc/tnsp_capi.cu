@@ -25,6 +25,36 @@ __global__ void reduce_slots(const double* __restrict__ src, int nslots, long lo
   }
 }
 
+// y[s] = sum_p H[s][p] x[p] over the kept hole rows: one block per row, fixed-order reduction
+__global__ void holes_gemv_rows(const double* __restrict__ H, long long np, long long rows, const double* __restrict__ x,
+                                double* __restrict__ y) {
+  __shared__ double red[8];
+  for (long long s = blockIdx.x; s < rows; s += gridDim.x) {
+    const double* h = H + s * np;
+    double acc = 0.0;
+    for (long long p = threadIdx.x; p < np; p += blockDim.x) acc = fma(h[p], x[p], acc);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+      y[s] = t;
+    }
+    __syncthreads();
+  }
+}
+
+// y[p] = sum_s H[s][p] u[s]: one thread per parameter, rows in order (coalesced along a row)
+__global__ void holes_gemv_cols(const double* __restrict__ H, long long np, long long rows, const double* __restrict__ u,
+                                double* __restrict__ y) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < np; p += (long long)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (long long s = 0; s < rows; ++s) acc = fma(H[s * np + p], u[s], acc);
+    y[p] = acc;
+  }
+}
+
 template <class T> __global__ void fill_ones(T* p) {
   if (threadIdx.x == 0 && blockIdx.x == 0) p[0] = (T)1;
 }
@@ -90,6 +120,10 @@ void free_chains(tnsp_ctx* c) {
   dfree(c->d_rec);
   c->rec_cap = 0;
   c->rec_n = 0;
+  dfree(c->d_holes);
+  c->holes_rows = c->holes_cap = 0;
+  dfree(c->d_gemv);
+  c->gemv_cap = 0;
   c->B = 0;
 }
 
@@ -542,6 +576,7 @@ int tnsp_observer_reset(tnsp_ctx* ctx) {
   CK(cudaMemsetAsync(ctx->d_delta, 0, sizeof(double) * ctx->n_params * ctx->nslots, ctx->stream));
   CK(cudaMemsetAsync(ctx->d_edelta, 0, sizeof(double) * ctx->n_params * ctx->nslots, ctx->stream));
   ctx->rec_n = 0;
+  ctx->holes_rows = 0;
   return TNSP_OK;
 }
 
@@ -566,6 +601,27 @@ int tnsp_sweep(tnsp_ctx* ctx, int nsweeps, int observe) {
   Chains ch = make_chains(ctx);
   if (!observe) {
     ch.rec_eloc = ch.rec_logws = ch.rec_rw = nullptr;
+  }
+  const long long new_rows = (observe && ctx->keep_holes) ? (long long)nrec * ctx->B : 0;
+  if (new_rows > 0) {
+    // append after the rows kept since the last observer reset (grow by doubling, keep the old rows)
+    const long long need = ctx->holes_rows + new_rows;
+    if (need > ctx->holes_cap) {
+      const long long cap = std::max(need, 2 * ctx->holes_cap);
+      double* grown = nullptr;
+      CK(cudaMalloc((void**)&grown, sizeof(double) * (size_t)cap * ctx->n_params));
+      if (ctx->holes_rows > 0)
+        CK(cudaMemcpyAsync(grown, ctx->d_holes, sizeof(double) * (size_t)ctx->holes_rows * ctx->n_params,
+                           cudaMemcpyDeviceToDevice, ctx->stream));
+      CK(cudaStreamSynchronize(ctx->stream));
+      dfree(ctx->d_holes);
+      ctx->d_holes = grown;
+      ctx->holes_cap = cap;
+    }
+    CK(cudaMemsetAsync(ctx->d_holes + (size_t)ctx->holes_rows * ctx->n_params, 0,
+                       sizeof(double) * (size_t)new_rows * ctx->n_params, ctx->stream));
+    ch.rec_hole = ctx->d_holes;
+    ch.hole_row0 = ctx->holes_rows;
   }
   const int grid = ctx->nslots;
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
@@ -594,6 +650,51 @@ int tnsp_sweep(tnsp_ctx* ctx, int nsweeps, int observe) {
     snprintf(buf, sizeof buf, "device status 0x%x (see TNSP_ST_* bits)", st);
     return fail(ctx, TNSP_E_DEVICE, buf);
   }
+  ctx->holes_rows += new_rows;
+  return TNSP_OK;
+}
+
+int tnsp_holes_keep(tnsp_ctx* ctx, int enable) {
+  if (!ctx) return TNSP_E_ARG;
+  CK(cudaSetDevice(ctx->device));
+  ctx->keep_holes = enable != 0;
+  if (!ctx->keep_holes) {
+    dfree(ctx->d_holes);
+    ctx->holes_rows = ctx->holes_cap = 0;
+  }
+  return TNSP_OK;
+}
+
+int tnsp_holes_count(tnsp_ctx* ctx, int64_t* rows) {
+  if (!ctx || !rows) return TNSP_E_ARG;
+  *rows = ctx->holes_rows;
+  return TNSP_OK;
+}
+
+int tnsp_holes_gemv(tnsp_ctx* ctx, int transpose, const double* x, double* y) {
+  if (!ctx || !x || !y) return TNSP_E_ARG;
+  if (!ctx->holes_rows) return fail(ctx, TNSP_E_STATE, "no hole rows kept (tnsp_holes_keep before an observed sweep)");
+  CK(cudaSetDevice(ctx->device));
+  const long long rows = ctx->holes_rows, np = ctx->n_params;
+  const long long nx = transpose ? rows : np, ny = transpose ? np : rows;
+  if (ctx->gemv_cap < nx + ny) {
+    dfree(ctx->d_gemv);
+    CK(cudaMalloc((void**)&ctx->d_gemv, sizeof(double) * (size_t)(nx + ny)));
+    ctx->gemv_cap = nx + ny;
+  }
+  double* dx = ctx->d_gemv;
+  double* dy = ctx->d_gemv + nx;
+  CK(cudaMemcpyAsync(dx, x, sizeof(double) * (size_t)nx, cudaMemcpyHostToDevice, ctx->stream));
+  if (transpose) {
+    const int grid = (int)std::min<long long>((np + 255) / 256, 65535);
+    holes_gemv_cols<<<grid, 256, 0, ctx->stream>>>(ctx->d_holes, np, rows, dx, dy);
+  } else {
+    const int grid = (int)std::min<long long>(rows, 65535);
+    holes_gemv_rows<<<grid, 256, 0, ctx->stream>>>(ctx->d_holes, np, rows, dx, dy);
+  }
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(y, dy, sizeof(double) * (size_t)ny, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
   return TNSP_OK;
 }
 

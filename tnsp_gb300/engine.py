@@ -107,6 +107,25 @@ class Sampler:
                                         ptr(edelta, ctypes.c_double)), "tnsp_observer_read")
         return scalars, delta, edelta
 
+    def keep_holes(self, enable=True):
+        """Keep every observed sample's hole row on the device (for the natural gradient) until the
+        next reset_observer; False releases them."""
+        self._check(self.lib.tnsp_holes_keep(self.ctx, 1 if enable else 0), "tnsp_holes_keep")
+
+    def holes_count(self):
+        n = ctypes.c_int64()
+        self._check(self.lib.tnsp_holes_count(self.ctx, ctypes.byref(n)), "tnsp_holes_count")
+        return n.value
+
+    def holes_gemv(self, x, transpose=False):
+        """H x (x over the parameters) or H^T x (x over the kept samples), H = the kept hole rows."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        n_params = sum(self.lattice[l1, l2].size for l1, l2 in self.lattice.sites())
+        y = np.zeros(n_params if transpose else self.holes_count())
+        self._check(self.lib.tnsp_holes_gemv(self.ctx, 1 if transpose else 0, ptr(x, ctypes.c_double),
+                                             ptr(y, ctypes.c_double)), "tnsp_holes_gemv")
+        return y
+
     def read_samples(self, nsweeps):
         eloc = np.zeros((nsweeps, self.B))
         logws = np.zeros((nsweeps, self.B))

@@ -17,9 +17,10 @@ chains' samples without device work.  ``Observer.__call__`` therefore only check
 accumulation already happened on the device, and ``energy`` / ``gradient`` read the reduced
 accumulators.
 
-Only the features of the sweep / E_loc / gradient path are mirrored: no restricted subspace other
-than charge conservation, no custom hopping Hamiltonians, no extra observer sets, no natural
-gradient, no configuration cache (``NotImplementedError`` where the reference would accept them).
+Only the features of the sweep / E_loc / gradient / natural-gradient (conjugate gradient) path are
+mirrored: no restricted subspace other than charge conservation, no custom hopping Hamiltonians, no
+extra observer sets, no cached deltas or configurations, no pseudo-inverse natural gradient
+(``NotImplementedError`` where the reference would accept them).
 """
 import numpy as np
 
@@ -155,6 +156,10 @@ class SweepSampling:
             if self._engine._uploaded_version != self.owner.version:
                 self._engine.upload()
             self._engine.sweep(1, observe=observing)
+            if observing and observer._enable_natural:
+                eloc, _, reweight = self._engine.read_samples(1)
+                observer._samples_e.extend(eloc[0].tolist())
+                observer._samples_w.extend(reweight[0].tolist())
             conf, logp = self._engine.read_chains()
             self._buffer = [(float(np.exp(lp)), Configuration(self.owner, c), observing) for c, lp in zip(conf, logp)]
             self._buffer.reverse()
@@ -170,12 +175,15 @@ class Observer:
     def __init__(self, owner, *, observer_set=None, enable_energy=False, enable_gradient=False,
                  enable_natural_gradient=False, cache_natural_delta=None, cache_configuration=False,
                  restrict_subspace=None, classical_energy=None):
-        if observer_set or enable_natural_gradient or cache_natural_delta or cache_configuration or \
-                restrict_subspace is not None or classical_energy is not None:
-            raise NotImplementedError("only energy and gradient observation are supported")
+        if observer_set or cache_natural_delta or cache_configuration or restrict_subspace is not None or \
+                classical_energy is not None:
+            raise NotImplementedError("only energy, gradient and natural-gradient observation are supported")
         self.owner = owner
-        self._enable_energy = enable_energy or enable_gradient
-        self._enable_gradient = enable_gradient
+        self._enable_natural = bool(enable_natural_gradient)
+        self._enable_energy = enable_energy or enable_gradient or self._enable_natural
+        self._enable_gradient = enable_gradient or self._enable_natural
+        self._samples_e = []
+        self._samples_w = []
         self._engine = None
         self._count = 0
         self._scalars = None
@@ -188,6 +196,8 @@ class Observer:
         self._engine = None
         self._count = 0
         self._scalars = None
+        self._samples_e = []
+        self._samples_w = []
         self.owner._active_observer = self
         return self
 
@@ -195,6 +205,7 @@ class Observer:
         if self._engine is not None:
             raise RuntimeError("one observer context observes one SweepSampling")
         self._engine = engine
+        engine.keep_holes(self._enable_natural)
         engine.reset_observer()
 
     def __exit__(self, exc_type, exc_val, exc_tb):
@@ -240,6 +251,59 @@ class Observer:
             raise RuntimeError("gradient not enabled")
         scal = self._read()
         return self.owner.unflatten(gradient_from(scal, self._delta, self._edelta))
+
+    def natural_gradient_by_conjugate_gradient(self, step, error):
+        """``Observer.natural_gradient_by_conjugate_gradient``
+        (tetragono/tetragono/sampling_lattice/observer.py:576-675) for real tensors: conjugate gradient
+        on D^T D x = D^T E with D_s = (delta_s - <delta>) sqrt(w_s / W), E_s = (E_loc,s - <E>)
+        sqrt(w_s / W), stopped after ``step`` steps or when |r|^2 / |b|^2 < error^2; returns 2 x per site
+        (dense arrays).  The per-sample hole rows stay on the device: D v and D^T u are products with
+        them there (``tnsp_holes_gemv``), the vector updates run here as in the reference; under a
+        process group D^T u and |Dp|^2 are summed over the ranks, as the reference's MPI reductions do."""
+        if not self._enable_natural:
+            raise RuntimeError("natural gradient not enabled")
+        scal = self._read()
+        W = scal[1]
+        energy = scal[4] / W
+        delta = np.asarray(self._delta) / W
+        w = np.asarray(self._samples_w)
+        param = np.sqrt(w / W)
+        En = (np.asarray(self._samples_e) - energy) * param
+        eng = self._engine
+
+        def D(v):
+            return param * (eng.holes_gemv(v) - np.dot(delta, v))
+
+        def DT(u):
+            pu = param * u
+            r = eng.holes_gemv(pu, transpose=True) - delta * pu.sum()
+            (r,) = allreduce_sum([r])
+            return r
+
+        b = DT(En)
+        b_square = np.dot(b, b)
+        x = np.zeros_like(b)
+        r = b - DT(D(x))
+        p = r
+        r_square = np.dot(r, r)
+        t = 0
+        while True:
+            if t == step:
+                break
+            if error != 0.0 and error**2 > r_square / b_square:
+                break
+            Dp = D(p)
+            (dpdp,) = allreduce_sum([np.array([np.dot(Dp, Dp)])])
+            alpha = r_square / dpdp[0]
+            x = x + alpha * p
+            r = r - alpha * DT(Dp)
+            new_r_square = np.dot(r, r)
+            beta = new_r_square / r_square
+            r_square = new_r_square
+            p = r + beta * p
+            t += 1
+        self.natural_gradient_steps = t
+        return self.owner.unflatten(2 * x)
 
     @property
     def instability(self):
