@@ -54,11 +54,23 @@ FP64_NOMINAL_GFLOPS = 1250.0
 FP32_NOMINAL_GFLOPS = 152 * 128 * 2 * 2.07
 DD_FMA_INSTRUCTIONS = 24
 DD_NOMINAL_GFLOPS = FP32_NOMINAL_GFLOPS / DD_FMA_INSTRUCTIONS
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per chain-sample of the sweep kernel, from
+# one ncu capture of the timed launch (profiles/sweep_kernel_dd_launches_heis8x8u1.md: 2.21 TB for 456
+# chains); scaled by the chains of a launch
+MEASURED_DRAM_BYTES_PER_SAMPLE = {("heis8x8u1", "dd"): 2.21e12 / 456}
 
 
 def _jsonable(o):
     """numpy scalars and arrays in the result line"""
     return o.tolist() if hasattr(o, "tolist") else str(o)
+
+
+def _measured_hbm_gbs():
+    """HBM copy bandwidth of the GB300s (MEASURED_PEAKS.json beside this file), or None."""
+    try:
+        return float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
+    except Exception:
+        return None
 
 
 def make_lattice(w, seed=20240601):
@@ -304,6 +316,11 @@ def run_ours(args):
     achieved = float(flops.sum()) / args.steps / (avg_launch_ms * 1e-3) / 1e9
     if rank != 0:
         return
+    per_sample = MEASURED_DRAM_BYTES_PER_SAMPLE.get((args.workload, args.precision))
+    traffic = per_sample * B if per_sample else None
+    dram_gbs = traffic / (avg_launch_ms * 1e-3) / 1e9 if traffic else None
+    hbm = _measured_hbm_gbs()
+    dram_frac = dram_gbs / hbm if (dram_gbs and hbm) else None
     if prec == TNSP_FP64:
         bound, kname, peak = "fp64", "sweep_kernel<double>", FP64_NOMINAL_GFLOPS
         peak_src = "nominal GB300 FP64 1.25 TFLOP/s (MEASURED_PEAKS.json has no FP64 figure)"
@@ -353,10 +370,12 @@ def run_ours(args):
         "gpu_launches": args.steps,
         "roofline": {"bound": bound, "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GFLOP/s",
                      "frac": achieved / peak if peak else None, "peak_source": peak_src,
+                     "dram_gbs": dram_gbs, "dram_frac_of_measured_hbm": dram_frac,
                      "flops_per_launch": float(flops.sum()) / args.steps,
                      "flops_split": {"contract": flops[0] / args.steps, "qr": flops[1] / args.steps,
                                      "svd": flops[2] / args.steps, "strip": flops[3] / args.steps},
-                     "traffic": None,
+                     "traffic": traffic,
+                     "traffic_source": "ncu capture of the same workload (per launch, scaled by chains)" if traffic else None,
                      "phase_cycle_share": phase_share(cycles)},
         "cpu_baseline": cpu,
         "clocks": clocks.summary(),
