@@ -284,6 +284,17 @@ def run_natural_case(name, kind, L1, L2, D, cut, tensor_seed, chain_seeds, n_the
     print(f"{name}: natural gradient for {len(runs)} (step, error) settings, saved {os.path.getsize(path)} bytes")
 
 
+def run_checkpoint_case(name, kind, L1, L2, D, tensor_seed):
+    """The lattice of case `name` pickled by the reference (as gm_save does, utility.py:219-224) to
+    <name>_lattice.pkl: a checkpoint file for tests/test_checkpoint.py."""
+    import pickle
+    lattice = build_lattice(kind, L1, L2, D, tensor_seed)
+    path = os.path.join(HERE, f"{name}_lattice.pkl")
+    with open(path, "wb") as f:
+        pickle.dump(lattice, f)
+    print(f"{name}: lattice file saved {os.path.getsize(path)} bytes")
+
+
 def _same_shapes(holes, L1, L2):
     return False
 
@@ -292,12 +303,15 @@ def _pack_holes(holes, L1, L2):
     return [[dense_site(holes[l1][l2]) for l2 in range(L2)] for l1 in range(L1)]
 
 
-if __name__ == "__main__" and "--natural-only" not in sys.argv:
+if __name__ == "__main__" and "--natural-only" not in sys.argv and "--checkpoint-only" not in sys.argv:
     run_case("heis_no_3x3_D3_dc4", "no", 3, 3, 3, 4, 1234, [11, 12], 3, 5)
     run_case("heis_no_4x4_D4_dc16", "no", 4, 4, 4, 16, 2024, [21, 22], 4, 6)
     run_case("heis_no_4x4_D3_dc5", "no", 4, 4, 3, 5, 77, [31], 3, 5)
     run_case("heis_u1_4x4_D111_dc5", "u1", 4, 4, (1, 1, 1), 5, 4321, [41, 42], 3, 5)
     run_case("heis_u1_4x4_D222_dc8", "u1", 4, 4, (2, 2, 2), 8, 8765, [51], 2, 4)
-if __name__ == "__main__":
+if __name__ == "__main__" and "--checkpoint-only" in sys.argv:
+    run_checkpoint_case("heis_no_3x3_D3_dc4", "no", 3, 3, 3, 1234)
+    run_checkpoint_case("heis_u1_4x4_D111_dc5", "u1", 4, 4, (1, 1, 1), 4321)
+if __name__ == "__main__" and "--checkpoint-only" not in sys.argv:
     run_natural_case("heis_no_3x3_D3_dc4", "no", 3, 3, 3, 4, 1234, [11, 12], 3, 5, [(6, 0.0), (50, 1e-3)])
     run_natural_case("heis_u1_4x4_D111_dc5", "u1", 4, 4, (1, 1, 1), 5, 4321, [41, 42], 3, 5, [(6, 0.0), (50, 1e-3)])
