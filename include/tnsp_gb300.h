@@ -109,6 +109,15 @@ int tnsp_chains_init(tnsp_ctx* ctx, int B, const int32_t* configs, const uint64_
  */
 int tnsp_sweep(tnsp_ctx* ctx, int nsweeps, int observe);
 
+/*
+ * tnsp_sweep for n contexts (different lattices, bond dimensions, cuts, precisions; one device) as
+ * one CUDA graph launch: their sweep kernels run concurrently and fill each other's idle SMs.  Every
+ * context's results are those of tnsp_sweep; tnsp_last_timing of each reports the whole graph.  A
+ * failure status is reported through the first context that has one.
+ * No reference counterpart: the reference runs one lattice per process.
+ */
+int tnsp_sweep_batch(tnsp_ctx* const* ctxs, int n, int nsweeps, int observe);
+
 /* Zeroes the observer accumulators and the per-sample record (Observer.__enter__, observer.py:41-81). */
 int tnsp_observer_reset(tnsp_ctx* ctx);
 

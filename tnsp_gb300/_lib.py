@@ -24,6 +24,7 @@ _c_void_p = ctypes.c_void_p
 # name -> (restype, argtypes), exactly the declarations of include/tnsp_gb300.h
 SIGNATURES = {
     "tnsp_ctx_create": (ctypes.c_int, [ctypes.POINTER(_c_void_p), ctypes.c_int, _c_void_p]),
+    "tnsp_sweep_batch": (ctypes.c_int, [ctypes.POINTER(_c_void_p), ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "tnsp_holes_keep": (ctypes.c_int, [_c_void_p, ctypes.c_int]),
     "tnsp_holes_count": (ctypes.c_int, [_c_void_p, _c_i64_p]),
     "tnsp_holes_gemv": (ctypes.c_int, [_c_void_p, ctypes.c_int, _c_dbl_p, _c_dbl_p]),

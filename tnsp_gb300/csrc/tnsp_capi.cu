@@ -580,32 +580,44 @@ int tnsp_observer_reset(tnsp_ctx* ctx) {
   return TNSP_OK;
 }
 
-int tnsp_sweep(tnsp_ctx* ctx, int nsweeps, int observe) {
+namespace {
+
+// one sweep call, split so that tnsp_sweep_batch can enqueue several contexts into one graph
+struct SweepPlan {
+  Model md;
+  Chains ch;
+  int nrec = 0;
+  long long new_rows = 0;
+};
+
+// host-side preparation: buffers, per-sample records, kept hole rows (may allocate, enqueues memsets
+// on the context stream)
+int sweep_prepare(tnsp_ctx* ctx, int nsweeps, int observe, SweepPlan& p) {
   if (!ctx) return TNSP_E_ARG;
   if (!ctx->B) return fail(ctx, TNSP_E_STATE, "no chains");
   if (nsweeps < 0) return fail(ctx, TNSP_E_ARG, "negative sweep count");
   CK(cudaSetDevice(ctx->device));
   int r = ensure_slots(ctx);
   if (r) return r;
-  const int nrec = (nsweeps == 0 && observe) ? 1 : nsweeps;
+  p.nrec = (nsweeps == 0 && observe) ? 1 : nsweeps;
   if (observe) {
     // the per-sample record holds the samples of this call
-    if (ctx->rec_cap < nrec) {
+    if (ctx->rec_cap < p.nrec) {
       dfree(ctx->d_rec);
-      CK(cudaMalloc((void**)&ctx->d_rec, sizeof(double) * 3 * (size_t)std::max(1, nrec) * ctx->B));
-      ctx->rec_cap = std::max(1, nrec);
+      CK(cudaMalloc((void**)&ctx->d_rec, sizeof(double) * 3 * (size_t)std::max(1, p.nrec) * ctx->B));
+      ctx->rec_cap = std::max(1, p.nrec);
     }
-    ctx->rec_n = nrec;
+    ctx->rec_n = p.nrec;
   }
-  Model md = make_model(ctx);
-  Chains ch = make_chains(ctx);
+  p.md = make_model(ctx);
+  p.ch = make_chains(ctx);
   if (!observe) {
-    ch.rec_eloc = ch.rec_logws = ch.rec_rw = nullptr;
+    p.ch.rec_eloc = p.ch.rec_logws = p.ch.rec_rw = nullptr;
   }
-  const long long new_rows = (observe && ctx->keep_holes) ? (long long)nrec * ctx->B : 0;
-  if (new_rows > 0) {
+  p.new_rows = (observe && ctx->keep_holes) ? (long long)p.nrec * ctx->B : 0;
+  if (p.new_rows > 0) {
     // append after the rows kept since the last observer reset (grow by doubling, keep the old rows)
-    const long long need = ctx->holes_rows + new_rows;
+    const long long need = ctx->holes_rows + p.new_rows;
     if (need > ctx->holes_cap) {
       const long long cap = std::max(need, 2 * ctx->holes_cap);
       double* grown = nullptr;
@@ -619,30 +631,32 @@ int tnsp_sweep(tnsp_ctx* ctx, int nsweeps, int observe) {
       ctx->holes_cap = cap;
     }
     CK(cudaMemsetAsync(ctx->d_holes + (size_t)ctx->holes_rows * ctx->n_params, 0,
-                       sizeof(double) * (size_t)new_rows * ctx->n_params, ctx->stream));
-    ch.rec_hole = ctx->d_holes;
-    ch.hole_row0 = ctx->holes_rows;
+                       sizeof(double) * (size_t)p.new_rows * ctx->n_params, ctx->stream));
+    p.ch.rec_hole = ctx->d_holes;
+    p.ch.hole_row0 = ctx->holes_rows;
   }
+  return TNSP_OK;
+}
+
+// the sweep launch itself on stream st (no synchronisation: capturable)
+int sweep_enqueue(tnsp_ctx* ctx, const SweepPlan& p, int nsweeps, int observe, cudaStream_t st) {
+  if (p.nrec == 0) return TNSP_OK;
   const int grid = ctx->nslots;
-  CK(cudaEventRecord(ctx->ev0, ctx->stream));
-  if (nrec > 0) {
-    if (ctx->precision == TNSP_FP64)
-      launch_sweep_f64(grid, ctx->smem_bytes, ctx->stream, md, ch, ctx->slots, ctx->d_scratch, ctx->d_ones, nsweeps,
-                       observe, 0);
-    else if (ctx->precision == TNSP_DD)
-      launch_sweep_dd(grid, ctx->smem_bytes, ctx->stream, md, ch, ctx->slots, ctx->d_scratch, ctx->d_ones, nsweeps,
-                      observe, 0);
-    else
-      launch_sweep_f32(grid, ctx->smem_bytes, ctx->stream, md, ch, ctx->slots, ctx->d_scratch, ctx->d_ones, nsweeps,
-                       observe, 0);
-    CK(cudaGetLastError());
-  }
-  CK(cudaEventRecord(ctx->ev1, ctx->stream));
-  CK(cudaEventSynchronize(ctx->ev1));
-  float ms = 0;
-  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-  ctx->last_ms = ms;
-  ctx->last_launches = nrec > 0 ? 1 : 0;
+  if (ctx->precision == TNSP_FP64)
+    launch_sweep_f64(grid, ctx->smem_bytes, st, p.md, p.ch, ctx->slots, ctx->d_scratch, ctx->d_ones, nsweeps, observe,
+                     0);
+  else if (ctx->precision == TNSP_DD)
+    launch_sweep_dd(grid, ctx->smem_bytes, st, p.md, p.ch, ctx->slots, ctx->d_scratch, ctx->d_ones, nsweeps, observe,
+                    0);
+  else
+    launch_sweep_f32(grid, ctx->smem_bytes, st, p.md, p.ch, ctx->slots, ctx->d_scratch, ctx->d_ones, nsweeps, observe,
+                     0);
+  CK(cudaGetLastError());
+  return TNSP_OK;
+}
+
+// after the launch completed: the device status word
+int sweep_finish(tnsp_ctx* ctx, const SweepPlan& p) {
   int32_t st = 0;
   CK(cudaMemcpy(&st, ctx->d_status, sizeof(int32_t), cudaMemcpyDeviceToHost));
   if (st & (TNSP_ST_SVD_NOCONV | TNSP_ST_NONFINITE | TNSP_ST_UNSUPPORTED)) {
@@ -650,8 +664,102 @@ int tnsp_sweep(tnsp_ctx* ctx, int nsweeps, int observe) {
     snprintf(buf, sizeof buf, "device status 0x%x (see TNSP_ST_* bits)", st);
     return fail(ctx, TNSP_E_DEVICE, buf);
   }
-  ctx->holes_rows += new_rows;
+  ctx->holes_rows += p.new_rows;
   return TNSP_OK;
+}
+
+}  // namespace
+
+int tnsp_sweep(tnsp_ctx* ctx, int nsweeps, int observe) {
+  SweepPlan p;
+  int r = sweep_prepare(ctx, nsweeps, observe, p);
+  if (r) return r;
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  r = sweep_enqueue(ctx, p, nsweeps, observe, ctx->stream);
+  if (r) return r;
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  CK(cudaEventSynchronize(ctx->ev1));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  ctx->last_ms = ms;
+  ctx->last_launches = p.nrec > 0 ? 1 : 0;
+  return sweep_finish(ctx, p);
+}
+
+int tnsp_sweep_batch(tnsp_ctx* const* ctxs, int n, int nsweeps, int observe) {
+  if (!ctxs || n < 1) return TNSP_E_ARG;
+  tnsp_ctx* ctx = ctxs[0];  // error messages of the batch go to the first context
+  for (int i = 0; i < n; ++i)
+    if (!ctxs[i] || ctxs[i]->device != ctx->device) return fail(ctx, TNSP_E_ARG, "contexts must share one device");
+  std::vector<SweepPlan> plans(n);
+  for (int i = 0; i < n; ++i) {
+    int r = sweep_prepare(ctxs[i], nsweeps, observe, plans[i]);
+    if (r) return r;
+    CK(cudaStreamSynchronize(ctxs[i]->stream));  // its memsets precede the graph
+  }
+  CK(cudaSetDevice(ctx->device));
+  // capture: fork from a capture stream to one stream per context, one sweep launch each, join
+  struct Res {
+    cudaStream_t cs = nullptr;
+    std::vector<cudaStream_t> side;
+    cudaEvent_t fork = nullptr, t0 = nullptr, t1 = nullptr;
+    std::vector<cudaEvent_t> join;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    ~Res() {
+      if (exec) cudaGraphExecDestroy(exec);
+      if (graph) cudaGraphDestroy(graph);
+      for (auto e : join) if (e) cudaEventDestroy(e);
+      for (auto e : {fork, t0, t1}) if (e) cudaEventDestroy(e);
+      for (auto s : side) if (s) cudaStreamDestroy(s);
+      if (cs) cudaStreamDestroy(cs);
+    }
+  } res;
+  res.side.assign(n, nullptr);
+  res.join.assign(n, nullptr);
+  CK(cudaStreamCreateWithFlags(&res.cs, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&res.fork, cudaEventDisableTiming));
+  CK(cudaEventCreate(&res.t0));
+  CK(cudaEventCreate(&res.t1));
+  for (int i = 0; i < n; ++i) {
+    CK(cudaStreamCreateWithFlags(&res.side[i], cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&res.join[i], cudaEventDisableTiming));
+  }
+  CK(cudaStreamBeginCapture(res.cs, cudaStreamCaptureModeThreadLocal));
+  int launched = 0, r = TNSP_OK;
+  if (cudaEventRecord(res.fork, res.cs) != cudaSuccess) r = fail(ctx, TNSP_E_CUDA, "fork event");
+  for (int i = 0; i < n && r == TNSP_OK; ++i) {
+    if (cudaStreamWaitEvent(res.side[i], res.fork, 0) != cudaSuccess) {
+      r = fail(ctx, TNSP_E_CUDA, "fork wait");
+      break;
+    }
+    r = sweep_enqueue(ctxs[i], plans[i], nsweeps, observe, res.side[i]);
+    launched += plans[i].nrec > 0 ? 1 : 0;
+    if (r == TNSP_OK && (cudaEventRecord(res.join[i], res.side[i]) != cudaSuccess ||
+                         cudaStreamWaitEvent(res.cs, res.join[i], 0) != cudaSuccess))
+      r = fail(ctx, TNSP_E_CUDA, "join");
+  }
+  const cudaError_t ec = cudaStreamEndCapture(res.cs, &res.graph);
+  if (r) return r;
+  if (ec != cudaSuccess) return fail(ctx, TNSP_E_CUDA, std::string("stream capture: ") + cudaGetErrorString(ec));
+  CK(cudaGraphInstantiate(&res.exec, res.graph, 0));
+  CK(cudaEventRecord(res.t0, res.cs));
+  CK(cudaGraphLaunch(res.exec, res.cs));
+  CK(cudaEventRecord(res.t1, res.cs));
+  CK(cudaEventSynchronize(res.t1));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, res.t0, res.t1));
+  int first = TNSP_OK;
+  for (int i = 0; i < n; ++i) {
+    ctxs[i]->last_ms = ms;
+    ctxs[i]->last_launches = launched;
+    const int ri = sweep_finish(ctxs[i], plans[i]);
+    if (ri && first == TNSP_OK) {
+      first = ri;
+      if (i) ctx->err = ctxs[i]->err;
+    }
+  }
+  return first;
 }
 
 int tnsp_holes_keep(tnsp_ctx* ctx, int enable) {

@@ -94,6 +94,18 @@ class Sampler:
             raise TnspError("lattice changed since upload; call upload() and init_chains() again")
         self._check(self.lib.tnsp_sweep(self.ctx, nsweeps, 1 if observe else 0), "tnsp_sweep")
 
+    @staticmethod
+    def sweep_batch(samplers, nsweeps=1, observe=False):
+        """``sweep`` of several samplers (different lattices; one device) as one CUDA graph launch in
+        which their kernels run concurrently."""
+        samplers = list(samplers)
+        for s in samplers:
+            if s._uploaded_version != s.lattice.version:
+                raise TnspError("lattice changed since upload; call upload() and init_chains() again")
+        arr = (ctypes.c_void_p * len(samplers))(*[s.ctx.value for s in samplers])
+        code = samplers[0].lib.tnsp_sweep_batch(arr, len(samplers), nsweeps, 1 if observe else 0)
+        samplers[0]._check(code, "tnsp_sweep_batch")
+
     def reset_observer(self):
         self._check(self.lib.tnsp_observer_reset(self.ctx), "tnsp_observer_reset")
 
