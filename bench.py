@@ -49,10 +49,10 @@ WORKLOADS = {
 DEFAULT_WORKLOAD = "heis8x8u1"
 FP64_NOMINAL_GFLOPS = 1250.0
 # FP32 pipe: 152 SMs x 128 FMA/clk x 2 flops x 2.07 GHz; one double-float multiply-add (the sampler's
-# inner operation in TNSP_DD mode: 1 FMUL + 3 FFMA + 20 FADD) issues 24 FP32 instructions, so its flop
-# peak is 1/24 of the FP32 flop rate
+# inner operation in TNSP_DD mode: 1 FMUL + 3 FFMA + 11 FADD) issues 15 FP32 instructions, so its flop
+# peak is 1/15 of the FP32 flop rate
 FP32_NOMINAL_GFLOPS = 152 * 128 * 2 * 2.07
-DD_FMA_INSTRUCTIONS = 24
+DD_FMA_INSTRUCTIONS = 15
 DD_NOMINAL_GFLOPS = FP32_NOMINAL_GFLOPS / DD_FMA_INSTRUCTIONS
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per chain-sample of the sweep kernel, from
 # one ncu capture of the timed launch (profiles/sweep_kernel_dd_launches_heis8x8u1.md: 2.21 TB for 456
