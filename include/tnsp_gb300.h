@@ -118,6 +118,13 @@ int tnsp_sweep(tnsp_ctx* ctx, int nsweeps, int observe);
  */
 int tnsp_sweep_batch(tnsp_ctx* const* ctxs, int n, int nsweeps, int observe);
 
+/*
+ * Replaces the configurations of all chains (configs as in tnsp_chains_init), keeping each chain's
+ * random-number stream: the next tnsp_sweep starts from them (e.g. after accepted proposals of a
+ * learned sampler).  No reference counterpart (the reference's chains only move by local sweeps).
+ */
+int tnsp_chains_write(tnsp_ctx* ctx, const int32_t* configs);
+
 /* Zeroes the observer accumulators and the per-sample record (Observer.__enter__, observer.py:41-81). */
 int tnsp_observer_reset(tnsp_ctx* ctx);
 
@@ -195,6 +202,29 @@ int tnsp_counters_read(tnsp_ctx* ctx, double* flops, int reset);
  */
 int tnsp_amplitude_noalloc(int L1, int L2, int P, const int* dims, const double* tensors, int cut, int B,
                            const int32_t* configs, double* mantissa, int32_t* exponent, void* stream);
+
+/*
+ * Learned proposal (no reference counterpart): an autoregressive masked MLP (MADE) over n_sites binary
+ * sites, x -> relu(W1 x + b1) -> relu(W2 h1 + b2) -> logits W3 h2 + b3 with p(x_i = 1 | x_<i) =
+ * sigmoid(logit_i); weights float32 (Adam), used as bfloat16, float32 accumulation; hand-written
+ * training and sampling kernels.  configs are 0/1 per site, [B][n_sites], B <= batch_capacity.
+ *   tnsp_made_train: one Adam step (learning rate lr) on the mean negative log-likelihood of the
+ *     batch; *loss = that mean before the step.
+ *   tnsp_made_gradient: the gradient of that loss (float32, parameter order of tnsp_made_params).
+ *   tnsp_made_logq: log q(x) per configuration.
+ *   tnsp_made_sample: B independent configurations drawn site by site, with their log q.
+ *   tnsp_made_params: read (write == 0) or replace the float32 parameters, in the order
+ *     W1 [hidden][n], b1 [hidden], W2 [hidden][hidden], b2 [hidden], W3 [n][hidden], b3 [n].
+ */
+typedef struct tnsp_made tnsp_made;
+int tnsp_made_create(tnsp_made** out, int device, int n_sites, int hidden, uint64_t seed, int batch_capacity);
+int tnsp_made_destroy(tnsp_made* made);
+const char* tnsp_made_error(tnsp_made* made);
+int tnsp_made_params(tnsp_made* made, float* params, int write);
+int tnsp_made_train(tnsp_made* made, const int32_t* configs, int B, double lr, double* loss);
+int tnsp_made_gradient(tnsp_made* made, const int32_t* configs, int B, float* grad);
+int tnsp_made_logq(tnsp_made* made, const int32_t* configs, int B, double* logq);
+int tnsp_made_sample(tnsp_made* made, int B, int32_t* configs, double* logq);
 
 #ifdef __cplusplus
 }

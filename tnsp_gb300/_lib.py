@@ -25,6 +25,16 @@ _c_void_p = ctypes.c_void_p
 SIGNATURES = {
     "tnsp_ctx_create": (ctypes.c_int, [ctypes.POINTER(_c_void_p), ctypes.c_int, _c_void_p]),
     "tnsp_sweep_batch": (ctypes.c_int, [ctypes.POINTER(_c_void_p), ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "tnsp_chains_write": (ctypes.c_int, [_c_void_p, _c_i32_p]),
+    "tnsp_made_create": (ctypes.c_int, [ctypes.POINTER(_c_void_p), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_uint64, ctypes.c_int]),
+    "tnsp_made_destroy": (ctypes.c_int, [_c_void_p]),
+    "tnsp_made_error": (ctypes.c_char_p, [_c_void_p]),
+    "tnsp_made_params": (ctypes.c_int, [_c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
+    "tnsp_made_train": (ctypes.c_int, [_c_void_p, _c_i32_p, ctypes.c_int, ctypes.c_double, _c_dbl_p]),
+    "tnsp_made_gradient": (ctypes.c_int, [_c_void_p, _c_i32_p, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
+    "tnsp_made_logq": (ctypes.c_int, [_c_void_p, _c_i32_p, ctypes.c_int, _c_dbl_p]),
+    "tnsp_made_sample": (ctypes.c_int, [_c_void_p, ctypes.c_int, _c_i32_p, _c_dbl_p]),
     "tnsp_holes_keep": (ctypes.c_int, [_c_void_p, ctypes.c_int]),
     "tnsp_holes_count": (ctypes.c_int, [_c_void_p, _c_i64_p]),
     "tnsp_holes_gemv": (ctypes.c_int, [_c_void_p, ctypes.c_int, _c_dbl_p, _c_dbl_p]),

@@ -566,6 +566,17 @@ int tnsp_chains_init(tnsp_ctx* ctx, int B, const int32_t* configs, const uint64_
   return ensure_slots(ctx);
 }
 
+int tnsp_chains_write(tnsp_ctx* ctx, const int32_t* configs) {
+  if (!ctx || !configs) return TNSP_E_ARG;
+  if (!ctx->B) return fail(ctx, TNSP_E_STATE, "no chains");
+  const long long n = (long long)ctx->B * ctx->L1 * ctx->L2;
+  for (long long i = 0; i < n; ++i)
+    if (configs[i] < 0 || configs[i] >= ctx->P) return fail(ctx, TNSP_E_ARG, "configuration index out of range");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaMemcpy(ctx->d_conf, configs, sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+  return TNSP_OK;
+}
+
 int tnsp_observer_reset(tnsp_ctx* ctx) {
   if (!ctx) return TNSP_E_ARG;
   if (!ctx->B) return fail(ctx, TNSP_E_STATE, "no chains");

@@ -147,6 +147,11 @@ class Sampler:
                                        ptr(rw, ctypes.c_double)), "tnsp_samples_read")
         return eloc, logws, rw
 
+    def write_chains(self, configs):
+        """Replaces every chain's configuration (random-number streams unchanged)."""
+        configs = np.ascontiguousarray(configs, dtype=np.int32).reshape(self.B, -1)
+        self._check(self.lib.tnsp_chains_write(self.ctx, ptr(configs, ctypes.c_int32)), "tnsp_chains_write")
+
     def read_chains(self):
         conf = np.zeros((self.B, self.lattice.L1, self.lattice.L2), dtype=np.int32)
         logp = np.zeros(self.B)
