@@ -639,6 +639,9 @@ template <class T> struct Engine : Chain<T> {
       }
       toc(PH_QR, t0);
       t0 = tic();
+      // the power-of-two normalisation is applied to the small factor R before the product instead
+      // of to the product (exact either way): the product is not read and written a second time
+      expo += block_normalize(Rb, (long long)rsz, red);
       // new T[i+1] (ktot x d'B') = R * T[i+1], sector by sector, into G; each thread owns a 4x4
       // output tile (4 rows of one sector's R x 4 columns), so one load of T feeds 4 FMAs
       const int dB = s_dd[i + 1] * s_dB[i + 1];
@@ -705,7 +708,6 @@ template <class T> struct Engine : Chain<T> {
         s_fl[i] = 0;
       }
       __syncthreads();
-      expo += block_normalize(Tbuf(s_buf[i + 1]), (long long)ktot * dB, red);
       toc(PH_RABSORB, t0);
     }
     // ---------------- truncating SVD sweep, per sector, global cut ----------------
@@ -919,6 +921,8 @@ template <class T> struct Engine : Chain<T> {
       __syncthreads();
       toc(PH_SVDOUT, t0);
       t0 = tic();
+      // U*S normalised before the absorption (exact; the product needs no second pass)
+      expo += block_normalize(Rb, (long long)rows * c, red);
       // new T[i-1] (A d x c) = T[i-1] * US, summing only over the rows of each kept vector's sector
       {
         const int Ad = s_dA[i - 1] * s_dd[i - 1];
@@ -957,7 +961,6 @@ template <class T> struct Engine : Chain<T> {
         s_dB[i - 1] = c;
       }
       __syncthreads();
-      expo += block_normalize(Tbuf(s_buf[i - 1]), (long long)s_dA[i - 1] * s_dd[i - 1] * c, red);
       toc(PH_USABSORB, t0);
     }
     if (n == 1) expo += block_normalize(Tbuf(s_buf[0]), (long long)s_dA[0] * s_dd[0] * s_dB[0], red);
