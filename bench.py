@@ -55,9 +55,9 @@ FP32_NOMINAL_GFLOPS = 152 * 128 * 2 * 2.07
 DD_FMA_INSTRUCTIONS = 15
 DD_NOMINAL_GFLOPS = FP32_NOMINAL_GFLOPS / DD_FMA_INSTRUCTIONS
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per chain-sample of the sweep kernel, from
-# one ncu capture of the timed launch (profiles/sweep_kernel_dd_launches_heis8x8u1.md: 2.21 TB for 456
-# chains); scaled by the chains of a launch
-MEASURED_DRAM_BYTES_PER_SAMPLE = {("heis8x8u1", "dd"): 2.21e12 / 456}
+# one ncu capture of the timed launch (profiles/sweep_kernel_dd_launches_heis8x8u1.md: 0.779 + 0.873 TB
+# for 456 chains); scaled by the chains of a launch
+MEASURED_DRAM_BYTES_PER_SAMPLE = {("heis8x8u1", "dd"): (0.779428e12 + 0.873435e12) / 456}
 
 
 def _jsonable(o):
