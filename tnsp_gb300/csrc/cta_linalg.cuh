@@ -79,22 +79,6 @@ __device__ __forceinline__ void rotate_pair(dd c, dd s, dd& u, dd& v) {
   v = dd_lincomb(s, x, c, y);
 }
 
-// Rotates the element pairs (x[r], y[r]), r = lane, lane + 32, ... < n, two per step so that the
-// dependent chains of two elements interleave (the same arithmetic per element as one at a time).
-template <class T> __device__ __forceinline__ void rotate_vectors(T c, T s, T* x, T* y, int n, int lane) {
-  int r = lane;
-  for (; r + 32 < n; r += 64) {
-    T u0 = x[r], v0 = y[r], u1 = x[r + 32], v1 = y[r + 32];
-    rotate_pair(c, s, u0, v0);
-    rotate_pair(c, s, u1, v1);
-    x[r] = u0;
-    y[r] = v0;
-    x[r + 32] = u1;
-    y[r + 32] = v1;
-  }
-  if (r < n) rotate_pair(c, s, x[r], y[r]);
-}
-
 // Lane-group primitives of the Jacobi routines: a rotation pair is handled by a group of kJG lanes, so
 // a warp works on 32 / kJG pairs at once and the latency-bound parts of a pair step (the reductions
 // of its three dot products and the scalar angle computation) run for all of them in the same
@@ -108,7 +92,8 @@ template <int G, class T> __device__ __forceinline__ T group_sum(T v) {
   for (int o = G / 2; o > 0; o >>= 1) v = v + shfl_xor(v, o);
   return v;
 }
-// rotate_vectors for a G-lane group: elements r = sl, sl + G, ..., two per step
+// Rotates the element pairs (x[r], y[r]) of a G-lane group, r = sl, sl + G, ... < n, two per step so
+// that the dependent chains of two elements interleave (the same arithmetic per element).
 template <int G, class T> __device__ __forceinline__ void rotate_group(T c, T s, T* x, T* y, int n, int sl) {
   int r = sl;
   for (; r + G < n; r += 2 * G) {
@@ -197,38 +182,6 @@ template <class T> __device__ int block_normalize(T* x, long n, T* red) {
   for (long i = threadIdx.x; i < n; i += blockDim.x) x[i] *= s;
   __syncthreads();
   return e;
-}
-
-// C[m x n] = A[m x k] * B[k x n]; A has row stride lda, B row stride ldb, C row stride ldc.
-// Each thread owns a 2x2 register tile of C.
-template <class T>
-__device__ void block_gemm(int m, int n, int k, const T* __restrict__ A, int lda, const T* __restrict__ B, int ldb,
-                           T* __restrict__ C, int ldc) {
-  const int tm = (m + 1) >> 1, tn = (n + 1) >> 1;
-  const long tiles = (long)tm * tn;
-  for (long t = threadIdx.x; t < tiles; t += blockDim.x) {
-    const int i0 = (int)(t / tn) * 2, j0 = (int)(t % tn) * 2;
-    const bool i1ok = i0 + 1 < m, j1ok = j0 + 1 < n;
-    T c00 = 0, c01 = 0, c10 = 0, c11 = 0;
-    const T* a0 = A + (long)i0 * lda;
-    const T* a1 = A + (long)(i1ok ? i0 + 1 : i0) * lda;
-    for (int p = 0; p < k; ++p) {
-      const T* b = B + (long)p * ldb;
-      const T b0 = b[j0], b1 = j1ok ? b[j0 + 1] : (T)0;
-      const T x0 = a0[p], x1 = a1[p];
-      c00 = fma(x0, b0, c00);
-      c01 = fma(x0, b1, c01);
-      c10 = fma(x1, b0, c10);
-      c11 = fma(x1, b1, c11);
-    }
-    C[(long)i0 * ldc + j0] = c00;
-    if (j1ok) C[(long)i0 * ldc + j0 + 1] = c01;
-    if (i1ok) {
-      C[(long)(i0 + 1) * ldc + j0] = c10;
-      if (j1ok) C[(long)(i0 + 1) * ldc + j0 + 1] = c11;
-    }
-  }
-  __syncthreads();
 }
 
 // One-sided (Hestenes) Jacobi on nv vectors X[j][0..len) (vector-major), accumulating the same
