@@ -1,0 +1,53 @@
+"""bench.py's host-side logic: the integrated autocorrelation time, phase shares, JSON line helpers."""
+import json
+import os
+import sys
+
+import numpy as np
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+import bench  # noqa: E402
+
+
+def test_tau_int_of_independent_samples_is_one_half():
+    x = np.random.default_rng(0).normal(size=(400, 64))
+    assert abs(bench.tau_int(x) - 0.5) < 0.1
+
+
+def test_tau_int_of_an_ar1_process():
+    """x_t = a x_{t-1} + noise has tau_int = (1 + a) / (2 (1 - a)) (= 4.5 for a = 0.8)."""
+    rng = np.random.default_rng(1)
+    a, n, chains = 0.8, 4000, 32
+    x = np.zeros((n, chains))
+    for t in range(1, n):
+        x[t] = a * x[t - 1] + rng.normal(size=chains)
+    assert abs(bench.tau_int(x[200:]) - (1 + a) / (2 * (1 - a))) < 0.6
+
+
+def test_tau_int_short_series_floor():
+    assert bench.tau_int(np.ones((2, 4))) == 0.5
+    assert bench.tau_int(np.ones((10, 4))) == 0.5  # no variance
+
+
+def test_phase_share_ignores_event_count_slots():
+    cycles = np.arange(1.0, 13.0)
+    share = bench.phase_share(cycles)
+    assert abs(sum(share.values()) - 1.0) < 1e-12
+    assert set(share) == {n for n in bench.PHASE_NAMES if n is not None}
+
+
+def test_json_line_accepts_numpy_values():
+    line = json.dumps({"a": np.int32(2), "b": np.float64(0.5), "c": np.arange(3)}, default=bench._jsonable)
+    assert json.loads(line) == {"a": 2, "b": 0.5, "c": [0, 1, 2]}
+
+
+def test_reduce_over_ranks_without_a_group_is_identity():
+    assert bench.reduce_over_ranks(None, 3.5) == 3.5
+
+
+def test_workloads_are_consistent():
+    for name, w in bench.WORKLOADS.items():
+        assert w["precision"] in ("fp64", "dd", "fp32"), name
+        assert w["chains"] >= 1 and w["steps"] >= 1
+    assert bench.DEFAULT_WORKLOAD in bench.WORKLOADS
+    assert abs(bench.DD_NOMINAL_GFLOPS * bench.DD_FMA_INSTRUCTIONS - bench.FP32_NOMINAL_GFLOPS) < 1e-6
