@@ -422,7 +422,7 @@ def run_reference(args):
         "dtype": "f64",
         "data": "synthetic (seeded random PEPS, Neel start)",
         "config": {"workload": args.workload, "lattice": f"{w['L1']}x{w['L2']}", "D": w["D"], "sectors": w["sectors"],
-                   "Dcut": w["cut"], "parallelism": f"{cores} processes"},
+                   "Dcut": w["cut"], "precision": "fp64", "parallelism": f"{cores} processes"},
         "raw_samples_per_s": raw,
         "tau_int": tau,
         "cpu_baseline": {"value": value, "unit": "effective samples/s", "cores": cores, "kind": "port",
