@@ -1,0 +1,335 @@
+"""CPU restatement of tetragono's amplitudes and local energies for a fermionic PEPS, by exact graded
+contraction (test infrastructure only; the checker for fermionic lattices, never the product).
+
+* projection on the configuration: ``Configuration._get_shrinker`` / ``_shrink_configuration``
+  (tetragono/tetragono/sampling_lattice/lattice.py:291-339): the site tensor contracted over ``P0``
+  with a shrinker (legs ``P`` = [(s, 1)], ``Q`` = the conjugated physical edge, one element 1 at
+  Q = (-s, index), P = (s, 0)); the dimension-one leg ``P_{l1}_{l2}_0`` stays open and carries the
+  charge;
+* the amplitude ``<s|psi>`` = ``hole(())``: here the whole network of projected tensors contracted
+  exactly, row-major, with the graded contraction of ``oracle.fermi_tensor`` (which is independent
+  of the order in which a network is contracted, so that with a cut large enough for the reference's
+  boundary MPS to be exact the two agree up to the order of the open legs);
+* ``tensor_element`` (tetragono/tetragono/tensor_element.py:20-108): every nonzero element of a
+  Hamiltonian term as a one-element tensor with the term's names and arrows, keyed by the
+  conjugated input points and the output points;
+* E_loc (tetragono/tetragono/sampling_lattice/observer.py:344-392): per term and per output
+  configuration s', ``(ws / |ws|^2) . H(s', s) . conj(wss)`` contracted over ``T`` and every ``P``
+  leg, summed.
+"""
+import itertools
+
+import numpy as np
+
+from .fermi_tensor import FermiTensor
+
+PHYSICS = (((0, 1), (1, 1)), False)   # spinless fermion site: empty (charge 0), occupied (charge 1)
+
+
+def point(index):
+    """Edge point (symmetry, index in segment) of physical index 0 / 1 on [(0, 1), (1, 1)]."""
+    return (int(index), 0)
+
+
+def shrink(site, l1, l2, index):
+    """lattice.py:306-339 for the single orbit 0."""
+    sym, k = point(index)
+    conj = (tuple((-s, d) for s, d in PHYSICS[0]), not PHYSICS[1])
+    shrinker = FermiTensor(["P", "Q"], [(((sym, 1),), False), conj])
+    shrinker[{"Q": (-sym, k), "P": (sym, 0)}] = 1.0
+    return site.contract(shrinker.edge_rename({"P": f"P_{l1}_{l2}_0"}), {("P0", "Q")})
+
+
+def _bond_names(l1, l2):
+    return {"R": f"H{l1}.{l2}", "L": f"H{l1}.{l2 - 1}", "D": f"V{l1}.{l2}", "U": f"V{l1 - 1}.{l2}"}
+
+
+def amplitude(sites, conf):
+    """The amplitude tensor (legs T and every P_{l1}_{l2}_0) of configuration ``conf[l1][l2]``."""
+    L1, L2 = len(sites), len(sites[0])
+    acc = None
+    for l1, l2 in itertools.product(range(L1), range(L2)):
+        t = shrink(sites[l1][l2], l1, l2, conf[l1][l2]).edge_rename(_bond_names(l1, l2))
+        if acc is None:
+            acc = t
+            continue
+        shared = {(n, n) for n in t.names if n in acc.names}
+        acc = acc.contract(t, shared)
+    return acc
+
+
+def value(ws, names):
+    """The element of amplitude tensor ``ws`` with its legs in the order ``names``."""
+    return float(ws.transpose(list(names)).scalar())
+
+
+def element_table(H):
+    """tensor_element.py:72-108 for a term whose legs all have one-dimensional segments."""
+    body = len(H.names) // 2
+    table = {}
+    for combo, sl in H._blocks():
+        block = H.data[sl]
+        for idx in itertools.product(*[range(n) for n in block.shape]):
+            v = block[idx]
+            if v == 0:
+                continue
+            points = [(H.edges[i][0][combo[i]][0], idx[i]) for i in range(len(H.names))]
+            edges = [(((points[i][0], 1),), H.edges[i][1]) for i in range(len(H.names))]
+            elem = FermiTensor(H.names, edges, H.group, np.full((1,) * len(H.names), v))
+            key_in = tuple((-points[H.names.index(f"I{i}")][0], points[H.names.index(f"I{i}")][1]) for i in range(body))
+            key_out = tuple(points[H.names.index(f"O{i}")] for i in range(body))
+            table.setdefault(key_in, {})[key_out] = elem
+    return table
+
+
+def local_energy(sites, terms, conf):
+    """E_loc of configuration ``conf`` (observer.py:344-392); ``terms`` = [(positions, H)], positions
+    ((l1, l2, 0), ...)."""
+    L1, L2 = len(sites), len(sites[0])
+    ws = amplitude(sites, conf)
+    if ws.norm_max() == 0:
+        return None
+    inv = ws / ws.norm_2()**2
+    all_names = {(n, n) for n in ws.names}
+    total = 0.0
+    for positions, H in terms:
+        table = element_table(H)
+        here = tuple(point(conf[l1][l2]) for l1, l2, _ in positions)
+        if here not in table:
+            continue
+        pnames = [f"P_{l1}_{l2}_{o}" for l1, l2, o in positions]
+        for out, elem in table[here].items():
+            new = [list(r) for r in conf]
+            for (l1, l2, _), (sym, _k) in zip(positions, out):
+                new[l1][l2] = sym
+            wss = amplitude(sites, new)
+            if wss.norm_max() == 0:
+                continue
+            v = inv.contract(elem, {(pnames[i], f"I{i}") for i in range(len(positions))})
+            v = v.edge_rename({f"O{i}": pnames[i] for i in range(len(positions))})
+            total += float(v.contract(wss.conjugate(), all_names).scalar())
+    return total
+
+
+# ----------------------------------------------------------------------------------------------
+# the same amplitudes as a bosonic network (what a dense boundary-MPS contraction evaluates)
+# ----------------------------------------------------------------------------------------------
+# A graded network contracted in a linear order of its legs equals the plain (bosonic) sum over
+# bond indices times, per index assignment, the product of: (-1)^p for every bond whose first leg
+# in that order has arrow False; (-1)^(p_e p_f) for every pair of bonds whose ends interleave; and
+# (-1)^(p_e * parity of the open legs between e's ends).  With the projected site legs in the
+# order (T, U, D, L, R, P) and the sites taken row-major, charge conservation of every prefix of
+# sites turns the non-local part into (a) a sign of the configuration alone and (b) a parity
+# operator on each site's D leg raised to the number of particles to its left in its row; the
+# rest is local to each site.  Taken column-major the same holds with the roles of the legs
+# exchanged.  Per site, on the projected slice (which is (-1)^n times the stored slice of the
+# occupation n, from the reversal of P0 when it is contracted with the shrinker):
+#
+#   row-major:    (-1)^( p_R (1 + n) + p_L p_D + p_D M_row )    M_row = particles left of the site
+#   column-major: (-1)^( p_D (1 + n) + p_D p_L + p_D p_R + p_L p_U + p_R M_col )
+#                                                               M_col = particles above the site
+#
+# and the configuration sign is prod over cuts k of (-1)^((N_<k + p_T)(N_<=k + p_T)), N counting
+# the particles of the rows (columns) before / up to k, p_T the parity of the T leg.  Boundary-MPS
+# truncation commutes with these signs: on every cut of a boundary line they are per-leg signs
+# times a function of the two sides' total parities, so singular values and kept subspaces are
+# those of the graded boundary state.
+
+ROW, COL = 0, 1
+_LEGS = ["U", "D", "L", "R"]
+
+
+def _leg_parities(site):
+    out = []
+    for x in _LEGS:
+        if x in site.names:
+            e = site.edge_by_name(x)
+            out.append(np.concatenate([np.full(d, (s & 1) == 1) for s, d in e[0]]).astype(np.int64))
+        else:
+            out.append(np.zeros(1, np.int64))
+    return out
+
+
+def leg_charges(site):
+    """Per-index U(1) charges of the U, D, L, R legs (1 entry 0 for a missing leg)."""
+    out = {}
+    for x in _LEGS:
+        if x in site.names:
+            out[x] = [s for s, d in site.edge_by_name(x)[0] for _ in range(d)]
+        else:
+            out[x] = [0]
+    return out
+
+
+def projected_dense(site, l1, l2, n):
+    """The graded projected tensor as a dense (u, d, l, r) array."""
+    t = shrink(site, l1, l2, n)
+    names = [x for x in ["T"] + _LEGS if x in t.names] + [f"P_{l1}_{l2}_0"]
+    t = t.transpose(names)
+    dims = [len(p) for p in _leg_parities(site)]
+    return t.data.reshape(dims)
+
+
+def bosonized_site(site, l1, l2, n, M, family):
+    d = projected_dense(site, l1, l2, n)
+    U, D, L, R = np.ix_(*_leg_parities(site))
+    if family == ROW:
+        e = (R * (1 - n)) ^ (L * D) ^ (D * (M & 1))
+    else:
+        e = (D * (1 - n)) ^ (D * L) ^ (D * R) ^ (L * U) ^ (R * (M & 1))
+    return np.where(e.astype(bool), -d, d)
+
+
+def prefix_counts(conf, family):
+    conf = np.asarray(conf)
+    if family == ROW:
+        return np.cumsum(conf, axis=1) - conf
+    return np.cumsum(conf, axis=0) - conf
+
+
+def configuration_sign(conf, p_T, family):
+    conf = np.asarray(conf)
+    N = conf.sum(axis=1) if family == ROW else conf.sum(axis=0)
+    s, before = 0, int(p_T)
+    for k in range(len(N) - 1):
+        upto = (before + int(N[k])) & 1
+        s ^= before & upto
+        before = upto
+    return -1.0 if s else 1.0
+
+
+def canonical_names(L1, L2, family):
+    sites = [(a, b) for a in range(L1) for b in range(L2)] if family == ROW else \
+            [(a, b) for b in range(L2) for a in range(L1)]
+    return ["T"] + [f"P_{a}_{b}_0" for a, b in sites]
+
+
+def amplitude_tensor(conf, value, T_symmetry, family):
+    """A one-element amplitude tensor with the open legs in the family's canonical order."""
+    conf = np.asarray(conf)
+    L1, L2 = conf.shape
+    names = canonical_names(L1, L2, family)
+    edges = [(((T_symmetry, 1),), False)] + [(((int(conf[int(n.split("_")[1]), int(n.split("_")[2])]), 1),), False)
+                                             for n in names[1:]]
+    return FermiTensor(names, edges, data=np.full((1,) * len(names), value))
+
+
+class BosonizedLattice:
+    """A fermionic lattice evaluated through the dense (bosonic) boundary-MPS oracle: per
+    configuration the projected slices carry the signs above, row-major for the row boundaries
+    (amplitude, horizontal replacements) and column-major for the column boundaries (vertical
+    replacements)."""
+
+    def __init__(self, sites, cut):
+        from .peps_oracle import DensePEPS
+        self.sites = sites
+        self.L1, self.L2 = len(sites), len(sites[0])
+        self.cut = cut
+        self.T_symmetry = sites[0][0].edge_by_name("T")[0][0][0]
+        self.p_T = self.T_symmetry & 1
+        legs = [[leg_charges(sites[a][b]) for b in range(self.L2)] for a in range(self.L1)]
+        flux = [[(-self.T_symmetry if (a, b) == (0, 0) else 0) for b in range(self.L2)] for a in range(self.L1)]
+        self.charges = (legs, [0, 1], flux)
+        self._DensePEPS = DensePEPS
+
+    def _peps(self, conf, family):
+        conf = np.asarray(conf)
+        M = prefix_counts(conf, family)
+        A = []
+        for a in range(self.L1):
+            row = []
+            for b in range(self.L2):
+                n = int(conf[a, b])
+                t = bosonized_site(self.sites[a][b], a, b, n, int(M[a, b]), family)
+                full = np.zeros((2,) + t.shape)
+                full[n] = t
+                row.append(full)
+            A.append(row)
+        return self._DensePEPS(A, [], self.cut, charges=self.charges)
+
+    def environments(self, conf):
+        from .peps_oracle import Environment
+        conf = np.asarray(conf)
+        return {f: Environment(self._peps(conf, f), conf) for f in (ROW, COL)}
+
+    def amplitude(self, envs):
+        conf = envs[ROW].conf
+        value = envs[ROW].amplitude() * configuration_sign(conf, self.p_T, ROW)
+        return amplitude_tensor(conf, value, self.T_symmetry, ROW)
+
+    def replace(self, envs, positions, new):
+        """``Configuration.replace`` of a nearest-neighbour pair as the reference dispatches it
+        (single_layer_auxiliaries.py:568-692): a row strip for a horizontal pair, a column strip for a
+        vertical one."""
+        conf = envs[ROW].conf
+        changed = [(p, s) for p, s in zip(positions, new) if conf[p[0], p[1]] != s]
+        if not changed:
+            return self.amplitude(envs)
+        (p0, s0), (p1, s1) = sorted(changed)
+        after = conf.copy()
+        after[p0[0], p0[1]], after[p1[0], p1[1]] = s0, s1
+        family = ROW if p0[0] == p1[0] else COL
+        env = envs[family]
+        M = prefix_counts(after, family)
+        for (a, b), s in ((p0[:2], s0), (p1[:2], s1)):
+            env.peps.A[a][b][s] = bosonized_site(self.sites[a][b], a, b, s, int(M[a, b]), family)
+        if family == ROW:
+            value = env.replace_horizontal(p0[0], p0[1], s0, s1)
+        else:
+            value = env.replace_vertical(p0[0], p0[1], s0, s1)
+        value *= configuration_sign(after, self.p_T, family)
+        return amplitude_tensor(after, value, self.T_symmetry, family)
+
+    def local_energy(self, terms, conf):
+        """E_loc through the bosonic environments, with the graded pairing of observer.py:378-383."""
+        conf = np.asarray(conf)
+        envs = self.environments(conf)
+        ws = self.amplitude(envs)
+        if ws.norm_max() == 0:
+            return None
+        return _pair_energy(ws, terms, conf, lambda positions, new: self.replace(envs, positions, new))
+
+
+def _pair_energy(ws, terms, conf, replaced):
+    inv = ws / ws.norm_2()**2
+    all_names = {(n, n) for n in ws.names}
+    total = 0.0
+    for positions, H in terms:
+        table = element_table(H)
+        here = tuple(point(conf[l1][l2]) for l1, l2, _ in positions)
+        if here not in table:
+            continue
+        pnames = [f"P_{l1}_{l2}_{o}" for l1, l2, o in positions]
+        for out, elem in table[here].items():
+            wss = replaced([p[:2] for p in positions], [sym for sym, _ in out])
+            if wss.norm_max() == 0:
+                continue
+            v = inv.contract(elem, {(pnames[i], f"I{i}") for i in range(len(positions))})
+            v = v.edge_rename({f"O{i}": pnames[i] for i in range(len(positions))})
+            total += float(v.contract(wss.conjugate(), all_names).scalar())
+    return total
+
+
+def hop_sign(conf, positions, new):
+    """The graded pairing of observer.py:378-383 for one term, in closed form, with both amplitudes
+    in the row-major canonical order: 1 for a diagonal element; for a particle moved between sites
+    i < j (row-major), (-1)^(particles strictly between them), times -1 when it moves from i to j."""
+    conf = np.asarray(conf)
+    L2 = conf.shape[1]
+    idx = [a * L2 + b for a, b in positions]
+    flat = conf.reshape(-1)
+    if all(flat[i] == s for i, s in zip(idx, new)):
+        return 1.0
+    i, j = sorted(idx)
+    between = int(flat[i + 1:j].sum()) & 1
+    forward = flat[i] == 1 and dict(zip(idx, new))[i] == 0
+    return (-1.0 if between else 1.0) * (-1.0 if forward else 1.0)
+
+
+def order_sign(conf, names_from, names_to, T_symmetry):
+    """Sign of reordering the one-element amplitude tensor's legs (only odd legs exchange)."""
+    conf = np.asarray(conf)
+    edges = [(((T_symmetry, 1),), False) if n == "T" else
+             (((int(conf[int(n.split("_")[1]), int(n.split("_")[2])]), 1),), False) for n in names_from]
+    t = FermiTensor(list(names_from), edges, data=np.ones((1,) * len(edges)))
+    return float(t.transpose(list(names_to)).scalar())

@@ -1,13 +1,18 @@
-"""Generates tests/golden/fermi_ops.npz: random fermionic tensors put through the reference's own
-TAT (the CPU build of ``oracle/build_ref.sh``) by every edge operation whose parity sign the oracle
-restates (transpose, reverse_edge, merge_edge, split_edge, conjugate, contract), for Fermi U(1) and
-Fermi Z2.
+"""Generates the fermionic golden vectors with the reference itself (its CPU build from
+``oracle/build_ref.sh`` and its tetragono / tetraku sources):
 
-    python tests/golden/make_fermi_golden.py
+* ``tests/golden/fermi_ops.npz``: random fermionic tensors put through the reference's TAT by every
+  edge operation whose parity sign the oracle restates (transpose, reverse_edge, merge_edge,
+  split_edge, conjugate, contract), for Fermi U(1) and Fermi Z2.  Each case stores the input tensors
+  (names, edges, block storage), the operation's arguments and the reference's output tensor.
+* ``tests/golden/tv_<case>.npz``: spinless-fermion t-V lattices built by tetraku's own plugin
+  (tetraku/tetraku/models/tV/__init__.py:23-76), seeded random site tensors, sweep chains of the
+  reference's ``SweepSampling`` and, per sample, the reference's amplitude tensor ``hole(())`` (its
+  leg order and element) and E_loc from its ``Observer``.
 
-Inputs are drawn from numpy's seeded generator; each case stores the input tensors (names, edges,
-block storage), the operation's arguments and the reference's output tensor.  Tests read the file
-without the reference.
+    python tests/golden/make_fermi_golden.py [--ops] [--tv] [REFERENCE_ROOT]
+
+Tests read the files without the reference.
 """
 import json
 import os
@@ -55,7 +60,7 @@ def storage_size(group, edges):
     return t.storage.size
 
 
-def main():
+def make_ops():
     rng = np.random.default_rng(20261204)
     cases, arrays = [], {}
 
@@ -134,5 +139,93 @@ def main():
     print(f"{len(cases)} cases -> {path}")
 
 
+def _tensor_record(t):
+    names = [str(n) for n in t.names]
+    edges = []
+    for n in t.names:
+        e = t.edge_by_name(n)
+        edges.append(([[int(sym.fermi), int(d)] for sym, d in list(e.segments)], bool(e.arrow)))
+    return {"names": names, "edges": edges}, np.array(t.storage, dtype=np.float64).copy()
+
+
+def run_tv_case(name, L1, L2, D, T, cut, tensor_seed, chain_seeds, n_therm, n_samples):
+    """Sweep chains of the reference on a t-V lattice (t = V = 1); records per sample the amplitude
+    tensor hole(()) and E_loc (observer.py:313-415)."""
+    sys.argv = sys.argv[:1] + [a for a in sys.argv[1:] if not a.startswith("--")]
+    import make_golden  # noqa: F401  (mpi4py stand-in and the reference's paths)
+    import tetragono as tet
+    from tetraku.models import tV
+
+    state = tV.abstract_lattice(L1, L2, D, T, 1.0, 1.0)
+    TAT.random.seed(tensor_seed)
+    lattice = tet.SamplingLattice(state)
+    for l1 in range(L1):
+        for l2 in range(L2):
+            t = lattice[l1, l2]
+            z = sum(1 for n in t.names if str(n) in ("U", "D", "L", "R"))
+            lattice[l1, l2] = t * (1.0 / np.sqrt(2.0 * (3 * D)**z))
+    out, meta = {}, {"name": name, "L1": L1, "L2": L2, "D": D, "T": T, "cut": cut, "tensor_seed": tensor_seed,
+                     "chain_seeds": chain_seeds, "n_therm": n_therm, "n_samples": n_samples, "sites": {},
+                     "terms": []}
+    for l1 in range(L1):
+        for l2 in range(L2):
+            desc, st = _tensor_record(lattice[l1, l2])
+            meta["sites"][f"{l1},{l2}"] = desc
+            out[f"site_{l1}_{l2}"] = st
+    for k, (positions, H) in enumerate(lattice._hamiltonians.items()):
+        desc, st = _tensor_record(H)
+        meta["terms"].append({"positions": [list(p) for p in positions], "tensor": desc})
+        out[f"term_{k}"] = st
+    # a start with T particles and nonzero amplitude: the first of a seeded run of random fillings
+    rng = np.random.default_rng(tensor_seed)
+    probe = tet.SweepSampling(lattice, cut, None, None)
+    while True:
+        occ = np.zeros(L1 * L2, dtype=np.int64)
+        occ[rng.choice(L1 * L2, size=T, replace=False)] = 1
+        start = occ.reshape(L1, L2, 1)
+        probe.configuration.import_configuration(start)
+        if probe.configuration.hole(()).norm_max() != 0:
+            break
+    observer = tet.Observer(lattice, enable_energy=True)
+    confs, poss, ws_names, ws_value, eloc = [], [], [], [], []
+    with observer:
+        for seed in chain_seeds:
+            TAT.random.seed(seed)
+            sampling = tet.SweepSampling(lattice, cut, None, None)
+            sampling.configuration.import_configuration(start)
+            for step in range(n_therm + n_samples):
+                possibility, configuration = sampling()
+                if step < n_therm:
+                    continue
+                before = observer._whole_result_reweight["energy"]
+                observer(possibility, configuration)
+                ws = configuration.hole(())
+                w = float(ws.storage[0])
+                reweight = w * w / possibility
+                confs.append(configuration.export_configuration()[:, :, 0].copy())
+                poss.append(possibility)
+                ws_names.append([str(n) for n in ws.names])
+                ws_value.append(w)
+                eloc.append((observer._whole_result_reweight["energy"] - before) / reweight)
+    meta["start"] = start[:, :, 0].tolist()
+    meta["ws_names"] = ws_names
+    out["confs"] = np.array(confs, dtype=np.int64)
+    out["possibility"] = np.array(poss)
+    out["ws"] = np.array(ws_value)
+    out["eloc"] = np.array(eloc)
+    energy, error = observer.energy
+    out["energy"] = np.array([energy, error])
+    out["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+    path = os.path.join(HERE, f"tv_{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"tv_{name}: {len(confs)} samples, E/site = {energy:.10f} +- {error:.2e}, {os.path.getsize(path)} bytes")
+
+
 if __name__ == "__main__":
-    main()
+    sys.path.insert(0, HERE)
+    both = "--ops" not in sys.argv and "--tv" not in sys.argv
+    if both or "--ops" in sys.argv:
+        make_ops()
+    if both or "--tv" in sys.argv:
+        run_tv_case("3x3_D1_T4_dc16", 3, 3, 1, 4, 16, 515, [61, 62], 3, 6)
+        run_tv_case("4x4_D2_T8_dc2", 4, 4, 2, 8, 2, 616, [71, 72], 3, 6)
