@@ -333,3 +333,97 @@ def order_sign(conf, names_from, names_to, T_symmetry):
              (((int(conf[int(n.split("_")[1]), int(n.split("_")[2])]), 1),), False) for n in names_from]
     t = FermiTensor(list(names_from), edges, data=np.ones((1,) * len(edges)))
     return float(t.transpose(list(names_to)).scalar())
+
+
+def hole_network(sites, conf, l1, l2):
+    """``hole(((l1, l2),))`` exactly (single_layer_auxiliaries.py:721-736): every projected tensor but
+    the one at (l1, l2), contracted; the bonds to (l1, l2) stay open, named as the reference names
+    them (``R0`` the left neighbour's R leg, ``L0`` the right neighbour's L leg, ``U0`` the lower
+    neighbour's U leg, ``D0`` the upper neighbour's D leg)."""
+    L1, L2 = len(sites), len(sites[0])
+    acc = None
+    for a, b in itertools.product(range(L1), range(L2)):
+        if (a, b) == (l1, l2):
+            continue
+        t = shrink(sites[a][b], a, b, conf[a][b]).edge_rename(_bond_names(a, b))
+        acc = t if acc is None else acc.contract(t, {(n, n) for n in t.names if n in acc.names})
+    return acc.edge_rename({f"H{l1}.{l2 - 1}": "R0", f"H{l1}.{l2}": "L0", f"V{l1 - 1}.{l2}": "D0", f"V{l1}.{l2}": "U0"})
+
+
+def holes(sites, conf):
+    """``Configuration.holes`` (lattice.py:362-416): <psi|s|d psi / d A[l1,l2]> / <psi|s|psi> as tensors
+    with the site's names and conjugated edges, expanded to the full physical leg by the shrinker."""
+    L1, L2 = len(sites), len(sites[0])
+    ws = amplitude(sites, conf)
+    inv_ws = (ws / ws.norm_2()**2).conjugate()
+    out = [[None] * L2 for _ in range(L1)]
+    for l1, l2 in itertools.product(range(L1), range(L2)):
+        h = hole_network(sites, conf, l1, l2)
+        own = f"P_{l1}_{l2}_0"
+        names = {(n, n) for n in ws.names if n != own and n in h.names}
+        h = h.contract(inv_ws, names)
+        h = h.edge_rename({"L0": "R", "R0": "L", "U0": "D", "D0": "U", own: "P0"})
+        sym, k = point(conf[l1][l2])
+        conj = (tuple((-s, d) for s, d in PHYSICS[0]), not PHYSICS[1])
+        shrinker = FermiTensor(["P", "Q"], [(((sym, 1),), False), conj])
+        shrinker[{"Q": (-sym, k), "P": (sym, 0)}] = 1.0
+        out[l1][l2] = h.contract(shrinker, {("P0", "P")}).edge_rename({"Q": "P0"})
+    return out
+
+
+# ----------------------------------------------------------------------------------------------
+# gradient through the bosonic holes
+# ----------------------------------------------------------------------------------------------
+# A hole H satisfies A . H = psi(A) / psi(A0), so in the site's leg order H[e] = kappa(e) *
+# (d psi / d A[e]) / psi, kappa the sign of TAT's full contraction of A with H:
+# (-1)^(n + p_T + p_D + p_R + [n_odd = 2 mod 4]) (the reversal of A's arrow-False legs and the merge
+# sign of its common group, contract.hpp:381-402, 487-500).  The gradient is conjugate(True) of a sum
+# of holes (observer.py:542-555, utility.py:230-231); on a tensor with the hole's arrows that
+# conjugation multiplies each block by the same kappa, so the two cancel: in the site's own leg order
+#
+#   gradient[n, e] = (-1)^(n + p_R (1 + n) + p_L p_D) * 2 (E Delta_B / W - E Delta_B / W)[n, e]
+#
+# where Delta_B accumulates the row-strip bosonic holes d psi_B / d B / psi_B, each multiplied by the
+# sample's own prefix parity (-1)^(p_D M_row) before it is added.
+
+
+def gradient_sign(site, n):
+    """(-1)^(n + p_R (1 + n) + p_L p_D) as a (u, d, l, r) array."""
+    U, D, L, R = np.ix_(*_leg_parities(site))
+    e = (n + R * (1 + n) + L * D) & 1
+    return np.where(e.astype(bool), -1.0, 1.0) * np.ones([len(p) for p in _leg_parities(site)])
+
+
+def signed_hole(lattice, envs, l1, l2):
+    """The row-strip bosonic hole of (l1, l2) divided by psi_B, with the prefix parity applied."""
+    env = envs[ROW]
+    h = env.site_hole(l1, l2) / env.amplitude()
+    M = int(prefix_counts(env.conf, ROW)[l1, l2])
+    pD = _leg_parities(lattice.sites[l1][l2])[1]
+    return np.where((pD[None, :, None, None] * (M & 1)).astype(bool), -h, h)
+
+
+def site_gradients(lattice, samples):
+    """Gradient tensors (dense (n, u, d, l, r) in the site's leg order) from samples of
+    (configuration, reweight, E_loc), as Observer.gradient forms them."""
+    L1, L2 = lattice.L1, lattice.L2
+    W = sum(rw for _, rw, _ in samples)
+    E = sum(rw * e for _, rw, e in samples) / W
+    out = []
+    for l1 in range(L1):
+        row = []
+        for l2 in range(L2):
+            shape = (2,) + tuple(len(p) for p in _leg_parities(lattice.sites[l1][l2]))
+            d, ed = np.zeros(shape), np.zeros(shape)
+            for conf, rw, e in samples:
+                envs = lattice.environments(conf)
+                h = signed_hole(lattice, envs, l1, l2)
+                n = int(np.asarray(conf)[l1, l2])
+                d[n] += rw * h
+                ed[n] += rw * e * h
+            g = 2 * (ed / W - E * d / W)
+            for n in (0, 1):
+                g[n] *= gradient_sign(lattice.sites[l1][l2], n)
+            row.append(g)
+        out.append(row)
+    return out

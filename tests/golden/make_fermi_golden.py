@@ -8,7 +8,8 @@
 * ``tests/golden/tv_<case>.npz``: spinless-fermion t-V lattices built by tetraku's own plugin
   (tetraku/tetraku/models/tV/__init__.py:23-76), seeded random site tensors, sweep chains of the
   reference's ``SweepSampling`` and, per sample, the reference's amplitude tensor ``hole(())`` (its
-  leg order and element) and E_loc from its ``Observer``.
+  leg order and element), E_loc from its ``Observer`` and the holes ``Configuration.holes()``; per
+  case the energy and the gradient.
 
     python tests/golden/make_fermi_golden.py [--ops] [--tv] [REFERENCE_ROOT]
 
@@ -186,8 +187,9 @@ def run_tv_case(name, L1, L2, D, T, cut, tensor_seed, chain_seeds, n_therm, n_sa
         probe.configuration.import_configuration(start)
         if probe.configuration.hole(()).norm_max() != 0:
             break
-    observer = tet.Observer(lattice, enable_energy=True)
+    observer = tet.Observer(lattice, enable_energy=True, enable_gradient=True)
     confs, poss, ws_names, ws_value, eloc = [], [], [], [], []
+    holes = {f"{a},{b}": [] for a in range(L1) for b in range(L2)}
     with observer:
         for seed in chain_seeds:
             TAT.random.seed(seed)
@@ -207,6 +209,12 @@ def run_tv_case(name, L1, L2, D, T, cut, tensor_seed, chain_seeds, n_therm, n_sa
                 ws_names.append([str(n) for n in ws.names])
                 ws_value.append(w)
                 eloc.append((observer._whole_result_reweight["energy"] - before) / reweight)
+                hs = configuration.holes()
+                for a in range(L1):
+                    for b in range(L2):
+                        desc, st = _tensor_record(hs[a][b])
+                        meta.setdefault("holes", {})[f"{a},{b}"] = desc
+                        holes[f"{a},{b}"].append(st)
     meta["start"] = start[:, :, 0].tolist()
     meta["ws_names"] = ws_names
     out["confs"] = np.array(confs, dtype=np.int64)
@@ -215,6 +223,15 @@ def run_tv_case(name, L1, L2, D, T, cut, tensor_seed, chain_seeds, n_therm, n_sa
     out["eloc"] = np.array(eloc)
     energy, error = observer.energy
     out["energy"] = np.array([energy, error])
+    out["total_weight"] = np.array(observer._total_weight)
+    grad = observer.gradient
+    meta["gradient"] = {}
+    for a in range(L1):
+        for b in range(L2):
+            out[f"holes_{a}_{b}"] = np.array(holes[f"{a},{b}"])
+            desc, st = _tensor_record(grad[a][b])
+            meta["gradient"][f"{a},{b}"] = desc
+            out[f"grad_{a}_{b}"] = st
     out["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
     path = os.path.join(HERE, f"tv_{name}.npz")
     np.savez_compressed(path, **out)

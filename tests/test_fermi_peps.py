@@ -107,3 +107,40 @@ def test_closed_form_term_sign_equals_the_graded_pairing():
                 assert pairing == h * fp.hop_sign(conf, [p[:2] for p in positions], new)
                 checked += 1
     assert checked > 1000
+
+
+def test_exact_graded_holes_match_reference():
+    z, meta, sites, _ = _load("3x3_D1_T4_dc16")
+
+    def mk(desc, st):
+        return FermiTensor(desc["names"], [([tuple(x) for x in segs], a) for segs, a in desc["edges"]]).set_storage(st)
+
+    for i, conf in enumerate(z["confs"][:4]):
+        hs = fp.holes(sites, conf)
+        for a in range(3):
+            for b in range(3):
+                ref = mk(meta["holes"][f"{a},{b}"], z[f"holes_{a}_{b}"][i])
+                mine = hs[a][b].transpose(ref.names)
+                assert mine.edges == ref.edges
+                assert np.abs(mine.data - ref.data).max() <= 1e-12 * np.abs(ref.data).max()
+
+
+@pytest.mark.parametrize("name", ["3x3_D1_T4_dc16", "4x4_D2_T8_dc2"])
+def test_gradient_from_bosonic_holes_matches_reference(name):
+    z, meta, sites, _ = _load(name)
+
+    def mk(desc, st):
+        return FermiTensor(desc["names"], [([tuple(x) for x in segs], a) for segs, a in desc["edges"]]).set_storage(st)
+
+    lat = fp.BosonizedLattice(sites, meta["cut"])
+    samples = [(np.asarray(c), z["ws"][i]**2 / z["possibility"][i], z["eloc"][i]) for i, c in enumerate(z["confs"])]
+    mine = fp.site_gradients(lat, samples)
+    refs = []
+    for a in range(meta["L1"]):
+        for b in range(meta["L2"]):
+            ref = mk(meta["gradient"][f"{a},{b}"], z[f"grad_{a}_{b}"])
+            legs = [x for x in ["T", "U", "D", "L", "R"] if x in ref.names]
+            refs.append((a, b, ref.transpose(["P0"] + legs).data.reshape(mine[a][b].shape)))
+    scale = max(np.abs(r).max() for _, _, r in refs)
+    for a, b, r in refs:
+        assert np.abs(mine[a][b] - r).max() <= 1e-12 * scale, (a, b)
