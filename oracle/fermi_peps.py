@@ -427,3 +427,62 @@ def site_gradients(lattice, samples):
             row.append(g)
         out.append(row)
     return out
+
+
+# ----------------------------------------------------------------------------------------------
+# E_loc from bosonic strip values and integer signs only
+# ----------------------------------------------------------------------------------------------
+def order_inversions(conf):
+    """Parity of the pairs of occupied sites that column-major and row-major orders put in opposite
+    order (a site strictly left of and below another): the sign of reordering the amplitude's odd
+    P legs from the column-major to the row-major canonical order."""
+    conf = np.asarray(conf)
+    L1, L2 = conf.shape
+    count = 0
+    for a, b in itertools.product(range(L1), range(L2)):
+        if conf[a, b]:
+            count += int(conf[:a, b + 1:].sum())
+    return count & 1
+
+
+def local_energy_signs(lattice, terms, conf):
+    """E_loc = sum over terms and outputs of h * hop_sign * sigma * psi_B(s') / psi_B(s), with psi_B(s)
+    the row-strip value, psi_B(s') the row-strip (horizontal pair) or column-strip (vertical pair)
+    replacement, and sigma = 1 for a horizontal pair, G_col(s') G_row(s) (-1)^inversions(s') for a
+    vertical one."""
+    conf = np.asarray(conf)
+    envs = lattice.environments(conf)
+    psi = envs[ROW].amplitude()
+    if psi == 0:
+        return None
+    g_row = configuration_sign(conf, lattice.p_T, ROW)
+    total = 0.0
+    for positions, H in terms:
+        table = element_table(H)
+        here = tuple(point(conf[a][b]) for a, b, _ in positions)
+        for out, elem in table.get(here, {}).items():
+            new = [sym for sym, _ in out]
+            pos = [p[:2] for p in positions]
+            h = float(elem.data.reshape(-1)[0])
+            changed = [(p, s) for p, s in zip(pos, new) if conf[p] != s]
+            if not changed:
+                total += h
+                continue
+            (p0, s0), (p1, s1) = sorted(changed)
+            after = conf.copy()
+            after[p0], after[p1] = s0, s1
+            family = ROW if p0[0] == p1[0] else COL
+            env = envs[family]
+            M = prefix_counts(after, family)
+            for (a, b), s in ((p0, s0), (p1, s1)):
+                env.peps.A[a][b][s] = bosonized_site(lattice.sites[a][b], a, b, s, int(M[a, b]), family)
+            if family == ROW:
+                wss = env.replace_horizontal(p0[0], p0[1], s0, s1)
+                sigma = 1.0
+            else:
+                wss = env.replace_vertical(p0[0], p0[1], s0, s1)
+                sigma = configuration_sign(after, lattice.p_T, COL) * g_row * (-1.0)**order_inversions(after)
+            if wss == 0.0:
+                continue
+            total += h * hop_sign(conf, pos, new) * sigma * wss / psi
+    return total

@@ -144,3 +144,21 @@ def test_gradient_from_bosonic_holes_matches_reference(name):
     scale = max(np.abs(r).max() for _, _, r in refs)
     for a, b, r in refs:
         assert np.abs(mine[a][b] - r).max() <= 1e-12 * scale, (a, b)
+
+
+@pytest.mark.parametrize("name", ["3x3_D1_T4_dc16", "4x4_D2_T8_dc2"])
+def test_local_energy_from_strip_values_and_integer_signs(name):
+    """The form a dense kernel evaluates: strip values of the bosonized lattice times signs computed
+    from particle counts alone."""
+    z, meta, sites, terms = _load(name)
+    lat = fp.BosonizedLattice(sites, meta["cut"])
+    for i, conf in enumerate(z["confs"]):
+        assert fp.local_energy_signs(lat, terms, conf) == pytest.approx(z["eloc"][i], rel=1e-12, abs=1e-12)
+
+
+def test_order_inversions_is_the_leg_reordering_sign():
+    rng = np.random.default_rng(11)
+    for _ in range(50):
+        conf = (rng.random((3, 4)) < 0.5).astype(int)
+        s = fp.order_sign(conf, fp.canonical_names(3, 4, fp.COL), fp.canonical_names(3, 4, fp.ROW), -int(conf.sum()))
+        assert s == (-1.0)**fp.order_inversions(conf)
