@@ -9,7 +9,8 @@
   (tetraku/tetraku/models/tV/__init__.py:23-76), seeded random site tensors, sweep chains of the
   reference's ``SweepSampling`` and, per sample, the reference's amplitude tensor ``hole(())`` (its
   leg order and element), E_loc from its ``Observer`` and the holes ``Configuration.holes()``; per
-  case the energy and the gradient.
+  case the energy and the gradient; for the 3x3 case also the lattice file the reference pickles
+  (``tv_<case>_lattice.pkl``).
 
     python tests/golden/make_fermi_golden.py [--ops] [--tv] [REFERENCE_ROOT]
 
@@ -149,7 +150,7 @@ def _tensor_record(t):
     return {"names": names, "edges": edges}, np.array(t.storage, dtype=np.float64).copy()
 
 
-def run_tv_case(name, L1, L2, D, T, cut, tensor_seed, chain_seeds, n_therm, n_samples):
+def run_tv_case(name, L1, L2, D, T, cut, tensor_seed, chain_seeds, n_therm, n_samples, save_lattice=False):
     """Sweep chains of the reference on a t-V lattice (t = V = 1); records per sample the amplitude
     tensor hole(()) and E_loc (observer.py:313-415)."""
     sys.argv = sys.argv[:1] + [a for a in sys.argv[1:] if not a.startswith("--")]
@@ -233,6 +234,10 @@ def run_tv_case(name, L1, L2, D, T, cut, tensor_seed, chain_seeds, n_therm, n_sa
             meta["gradient"][f"{a},{b}"] = desc
             out[f"grad_{a}_{b}"] = st
     out["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+    if save_lattice:
+        import pickle
+        with open(os.path.join(HERE, f"tv_{name}_lattice.pkl"), "wb") as f:
+            pickle.dump(lattice, f)
     path = os.path.join(HERE, f"tv_{name}.npz")
     np.savez_compressed(path, **out)
     print(f"tv_{name}: {len(confs)} samples, E/site = {energy:.10f} +- {error:.2e}, {os.path.getsize(path)} bytes")
@@ -244,5 +249,5 @@ if __name__ == "__main__":
     if both or "--ops" in sys.argv:
         make_ops()
     if both or "--tv" in sys.argv:
-        run_tv_case("3x3_D1_T4_dc16", 3, 3, 1, 4, 16, 515, [61, 62], 3, 6)
+        run_tv_case("3x3_D1_T4_dc16", 3, 3, 1, 4, 16, 515, [61, 62], 3, 6, save_lattice=True)
         run_tv_case("4x4_D2_T8_dc2", 4, 4, 2, 8, 2, 616, [71, 72], 3, 6)

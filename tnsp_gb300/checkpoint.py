@@ -8,14 +8,17 @@ tensors, edges and symmetries pickle their binary dump as state (PyTAT/PyTAT.hpp
 * tensor: ``b"TAT"``, u16 version (1), names, edges, storage;
 * names: u64 count, then per name a u64 length and its bytes;
 * edge: a u8 arrow for fermionic symmetries, then u64 count and ``count`` (symmetry, u64 dimension)
-  pairs of 16 bytes each (no symmetry: 8 bytes of padding; U(1): i32 charge and 4 bytes of padding);
+  pairs of 16 bytes each (no symmetry: 8 bytes of padding; Bose or Fermi U(1): i32 charge and 4 bytes
+  of padding);
 * storage: u64 count and ``count`` float64 values in TAT's block order.
 
 ``load_lattice`` reads such a file into stand-in objects (``RefSamplingLattice`` with ``RefTensor``
 / ``RefEdge`` / ``RefSymmetry`` members), ``to_sampling_lattice`` turns it into this package's
 ``SamplingLattice``, ``set_tensors`` writes dense site tensors back into the block storage, and
 ``save_lattice`` pickles the stand-ins under the reference's own class paths, so the reference loads
-the file unchanged.  Supported: real (float64) tensors without symmetry or with Bose U(1).
+the file unchanged.  Supported: real (float64) tensors without symmetry, with Bose U(1) or with
+Fermi U(1) (edges then carry their arrows; ``tnsp_gb300.fermion`` turns such a lattice into its
+dense form).
 
 Configuration files are the int64 files of ``write_configurations`` / ``read_configurations``
 (tetragono/tetragono/utility.py:390-418): a header [number of blocks, rank, *shape] followed by one
@@ -30,7 +33,9 @@ import numpy as np
 from .lattice import ORDER, SamplingLattice, block_to_dense, element_table, iterate_blocks, _segment_offsets, \
     site_charges
 
-_SYMMETRIES = {"No": 0, "BoseU1": 4}  # bytes of the symmetry value inside a 16-byte segment pair
+_SYMMETRIES = {"No": 0, "BoseU1": 4, "FermiU1": 4}  # bytes of the symmetry value in a 16-byte segment pair
+_CHARGED = ("BoseU1", "FermiU1")
+_FERMI = ("FermiU1",)
 
 
 def _u64(buf, pos):
@@ -47,48 +52,55 @@ class RefSymmetry:
         self.charge = charge
 
     def __setstate__(self, state):
-        self.charge = struct.unpack_from("<i", state, 0)[0] if self.symmetry == "BoseU1" else None
+        self.charge = struct.unpack_from("<i", state, 0)[0] if self.symmetry in _CHARGED else None
 
     def dumps(self):
-        return struct.pack("<i", self.charge) if self.symmetry == "BoseU1" else b"\x00"
+        return struct.pack("<i", self.charge) if self.symmetry in _CHARGED else b"\x00"
 
     def __reduce_ex__(self, protocol):
         return _newobj, (type(self),), self.dumps()
 
 
 class RefEdge:
-    """A TAT edge: segments [(charge, dimension), ...] (charge 0 without symmetry)."""
+    """A TAT edge: segments [(charge, dimension), ...] (charge 0 without symmetry) and, for a
+    fermionic symmetry, its arrow."""
     _ref_module = None
     _ref_name = "Edge"
     symmetry = "No"
 
-    def __init__(self, segments=()):
+    def __init__(self, segments=(), arrow=False):
         self.segments = [tuple(s) for s in segments]
+        self.arrow = bool(arrow)
 
     @classmethod
     def _parse(cls, buf, pos, symmetry):
+        arrow = False
+        if symmetry in _FERMI:
+            arrow = buf[pos] != 0
+            pos += 1
         count, pos = _u64(buf, pos)
         segments = []
         for _ in range(count):
-            charge = struct.unpack_from("<i", buf, pos)[0] if symmetry == "BoseU1" else 0
+            charge = struct.unpack_from("<i", buf, pos)[0] if symmetry in _CHARGED else 0
             dim = struct.unpack_from("<Q", buf, pos + 8)[0]
             segments.append((int(charge), int(dim)))
             pos += 16
-        return segments, pos
+        return segments, arrow, pos
 
     @staticmethod
-    def _pack(segments, symmetry):
-        out = [struct.pack("<Q", len(segments))]
+    def _pack(segments, symmetry, arrow=False):
+        out = [bytes([1 if arrow else 0])] if symmetry in _FERMI else []
+        out.append(struct.pack("<Q", len(segments)))
         for charge, dim in segments:
-            head = struct.pack("<i", charge) + b"\x00" * 4 if symmetry == "BoseU1" else b"\x00" * 8
+            head = struct.pack("<i", charge) + b"\x00" * 4 if symmetry in _CHARGED else b"\x00" * 8
             out.append(head + struct.pack("<Q", dim))
         return b"".join(out)
 
     def __setstate__(self, state):
-        self.segments, _ = RefEdge._parse(state, 0, self.symmetry)
+        self.segments, self.arrow, _ = RefEdge._parse(state, 0, self.symmetry)
 
     def dumps(self):
-        return RefEdge._pack(self.segments, self.symmetry)
+        return RefEdge._pack(self.segments, self.symmetry, self.arrow)
 
     def __reduce_ex__(self, protocol):
         return _newobj, (type(self),), self.dumps()
@@ -100,9 +112,10 @@ class RefTensor:
     _ref_name = "Tensor"
     symmetry = "No"
 
-    def __init__(self, names=(), edges=(), storage=()):
+    def __init__(self, names=(), edges=(), storage=(), arrows=None):
         self.names = list(names)
         self.edges = [list(e) for e in edges]
+        self.arrows = list(arrows) if arrows is not None else [False] * len(self.edges)
         self.storage = np.asarray(storage, dtype=np.float64)
 
     def __setstate__(self, state):
@@ -120,12 +133,13 @@ class RefTensor:
             names.append(buf[pos:pos + n].decode())
             pos += n
         count, pos = _u64(buf, pos)
-        edges = []
+        edges, arrows = [], []
         for _ in range(count):
-            segments, pos = RefEdge._parse(buf, pos, self.symmetry)
+            segments, arrow, pos = RefEdge._parse(buf, pos, self.symmetry)
             edges.append(segments)
+            arrows.append(arrow)
         count, pos = _u64(buf, pos)
-        self.names, self.edges = names, edges
+        self.names, self.edges, self.arrows = names, edges, arrows
         self.storage = np.frombuffer(buf, dtype="<f8", count=count, offset=pos).copy()
 
     def dumps(self):
@@ -134,8 +148,8 @@ class RefTensor:
             b = n.encode()
             out.append(struct.pack("<Q", len(b)) + b)
         out.append(struct.pack("<Q", len(self.edges)))
-        for e in self.edges:
-            out.append(RefEdge._pack(e, self.symmetry))
+        for e, a in zip(self.edges, self.arrows):
+            out.append(RefEdge._pack(e, self.symmetry, a))
         out.append(struct.pack("<Q", self.storage.size))
         out.append(np.ascontiguousarray(self.storage, dtype="<f8").tobytes())
         return b"".join(out)
@@ -182,10 +196,10 @@ def _ref_class(module, name):
     elif parts[0] == "TAT" and len(parts) >= 2 and parts[1] in _SYMMETRIES:
         base = {"Tensor": RefTensor, "Edge": RefEdge, "Symmetry": RefSymmetry}.get(name)
         if base is None or (name == "Tensor" and parts[2:] != ["D"]) or (name != "Tensor" and len(parts) != 2):
-            raise NotImplementedError(f"{module}.{name}: only float64 tensors without symmetry or with Bose U(1)")
+            raise NotImplementedError(f"{module}.{name}: only float64 tensors without symmetry, Bose or Fermi U(1)")
         cls = type(f"{parts[1]}{name}", (base,), {"_ref_module": module, "_ref_name": name, "symmetry": parts[1]})
     elif parts[0] in ("TAT", "tetragono"):
-        raise NotImplementedError(f"{module}.{name} is not supported (no symmetry or Bose U(1), float64 only)")
+        raise NotImplementedError(f"{module}.{name} is not supported (no symmetry, Bose or Fermi U(1), float64 only)")
     else:
         return None
     _CLASSES[key] = cls
@@ -257,6 +271,8 @@ def to_sampling_lattice(ref):
     st = ref.state
     L1, L2 = st["L1"], st["L2"]
     grid = st["_lattice"]
+    if getattr(type(grid[0][0]), "symmetry", "No") in _FERMI:
+        raise NotImplementedError("a fermionic lattice: use tnsp_gb300.fermion.from_reference_lattice")
     phys = st["_physics_edges"][0][0][0].segments
     P = sum(d for _, d in phys)
     tensors = [[None] * L2 for _ in range(L1)]
