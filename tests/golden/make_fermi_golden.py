@@ -251,3 +251,4 @@ if __name__ == "__main__":
     if both or "--tv" in sys.argv:
         run_tv_case("3x3_D1_T4_dc16", 3, 3, 1, 4, 16, 515, [61, 62], 3, 6, save_lattice=True)
         run_tv_case("4x4_D2_T8_dc2", 4, 4, 2, 8, 2, 616, [71, 72], 3, 6)
+        run_tv_case("3x4_D2_T5_dc3", 3, 4, 2, 5, 3, 717, [81, 82], 3, 6, save_lattice=True)
