@@ -53,7 +53,7 @@ def test_bosonized_boundary_mps_matches_reference(name):
 def test_truncation_is_active_in_the_truncated_cases(name):
     z, meta, sites, terms = _load(name)
     rel = [abs(fp.value(fp.amplitude(sites, c), meta["ws_names"][i]) / z["ws"][i] - 1) for i, c in enumerate(z["confs"])]
-    assert max(rel) > 1e-2
+    assert max(rel) > 1e-4   # truncation moves the amplitudes by far more than the 1e-12 parity tolerance
 
 
 def test_column_family_is_exact_without_truncation():
