@@ -486,3 +486,66 @@ def local_energy_signs(lattice, terms, conf):
                 continue
             total += h * hop_sign(conf, pos, new) * sigma * wss / psi
     return total
+
+
+def natural_gradient(lattice, samples, step, error):
+    """``natural_gradient_by_conjugate_gradient`` (observer.py:576-675) on the bosonic rows: each
+    sample's row is its prefix-signed row-strip holes laid out per site as (n, u, d, l, r); the
+    reference's rows are the same numbers up to one fixed sign and order per element, under which the
+    conjugate-gradient iteration is covariant, and its final ``conjugate(True)`` of the solution is
+    the same per-element fold as the gradient's."""
+    L1, L2 = lattice.L1, lattice.L2
+    shapes = [[(2,) + tuple(len(p) for p in _leg_parities(lattice.sites[a][b])) for b in range(L2)] for a in range(L1)]
+    sizes = [int(np.prod(shapes[a][b])) for a in range(L1) for b in range(L2)]
+    rows, W, EW = [], 0.0, 0.0
+    for conf, rw, e in samples:
+        envs = lattice.environments(conf)
+        parts = []
+        for a in range(L1):
+            for b in range(L2):
+                full = np.zeros(shapes[a][b])
+                full[int(np.asarray(conf)[a, b])] = signed_hole(lattice, envs, a, b)
+                parts.append(full.ravel())
+        rows.append(np.concatenate(parts))
+        W += rw
+        EW += rw * e
+    E = EW / W
+    rows = np.array(rows)
+    rw = np.array([s[1] for s in samples])
+    es = np.array([s[2] for s in samples])
+    delta = (rw[:, None] * rows).sum(axis=0) / W
+    param = np.sqrt(rw / W)
+    Delta = (rows - delta) * param[:, None]
+    Energy = (es - E) * param
+
+    def A(v):
+        return Delta.T @ (Delta @ v)
+
+    b = Delta.T @ Energy
+    b_square = float(b @ b)
+    x = np.zeros_like(b)
+    r = b - A(x)
+    p = r
+    r_square = float(r @ r)
+    t = 0
+    while t != step and not (error != 0.0 and error**2 > r_square / b_square):
+        Dp = Delta @ p
+        alpha = r_square / float(Dp @ Dp)
+        x = x + alpha * p
+        r = r - alpha * (Delta.T @ Dp)
+        new = float(r @ r)
+        p = r + (new / r_square) * p
+        r_square = new
+        t += 1
+    x = 2 * x
+    out, k = [], 0
+    for a in range(L1):
+        row = []
+        for b in range(L2):
+            g = x[k:k + sizes[a * L2 + b]].reshape(shapes[a][b]).copy()
+            k += sizes[a * L2 + b]
+            for n in (0, 1):
+                g[n] *= gradient_sign(lattice.sites[a][b], n)
+            row.append(g)
+        out.append(row)
+    return out

@@ -9,8 +9,8 @@
   (tetraku/tetraku/models/tV/__init__.py:23-76), seeded random site tensors, sweep chains of the
   reference's ``SweepSampling`` and, per sample, the reference's amplitude tensor ``hole(())`` (its
   leg order and element), E_loc from its ``Observer`` and the holes ``Configuration.holes()``; per
-  case the energy and the gradient; for the 3x3 case also the lattice file the reference pickles
-  (``tv_<case>_lattice.pkl``).
+  case the energy and the gradient; for some cases also the lattice file the reference pickles
+  (``tv_<case>_lattice.pkl``) and its natural gradient by conjugate gradient (``tv_<case>_natgrad.npz``).
 
     python tests/golden/make_fermi_golden.py [--ops] [--tv] [REFERENCE_ROOT]
 
@@ -243,6 +243,51 @@ def run_tv_case(name, L1, L2, D, T, cut, tensor_seed, chain_seeds, n_therm, n_sa
     print(f"tv_{name}: {len(confs)} samples, E/site = {energy:.10f} +- {error:.2e}, {os.path.getsize(path)} bytes")
 
 
+def run_tv_natural(name, L1, L2, D, T, cut, tensor_seed, chain_seeds, n_therm, n_samples, runs):
+    """The chains of t-V case ``name`` again, observed with enable_natural_gradient; saves the
+    reference's natural_gradient_by_conjugate_gradient(step, error) (observer.py:576-675) for every
+    (step, error) in ``runs`` to tv_<name>_natgrad.npz (one observed run per setting, since the
+    reference releases its per-sample deltas after one call)."""
+    sys.argv = sys.argv[:1] + [a for a in sys.argv[1:] if not a.startswith("--")]
+    import make_golden  # noqa: F401
+    import tetragono as tet
+    from tetraku.models import tV
+
+    state = tV.abstract_lattice(L1, L2, D, T, 1.0, 1.0)
+    TAT.random.seed(tensor_seed)
+    lattice = tet.SamplingLattice(state)
+    for l1 in range(L1):
+        for l2 in range(L2):
+            t = lattice[l1, l2]
+            z = sum(1 for n in t.names if str(n) in ("U", "D", "L", "R"))
+            lattice[l1, l2] = t * (1.0 / np.sqrt(2.0 * (3 * D)**z))
+    start = np.load(os.path.join(HERE, f"tv_{name}.npz"))
+    meta = json.loads(bytes(start["meta"]).decode())
+    conf0 = np.array(meta["start"], dtype=np.int64)[:, :, None]
+    out, desc = {"runs": np.array(runs, dtype=np.float64)}, {}
+    for k, (steps, error) in enumerate(runs):
+        observer = tet.Observer(lattice, enable_energy=True, enable_gradient=True, enable_natural_gradient=True)
+        with observer:
+            for seed in chain_seeds:
+                TAT.random.seed(seed)
+                sampling = tet.SweepSampling(lattice, cut, None, None)
+                sampling.configuration.import_configuration(conf0)
+                for step in range(n_therm + n_samples):
+                    possibility, configuration = sampling()
+                    if step >= n_therm:
+                        observer(possibility, configuration)
+        grad = observer.natural_gradient_by_conjugate_gradient(int(steps), float(error))
+        for l1 in range(L1):
+            for l2 in range(L2):
+                d, st = _tensor_record(grad[l1][l2])
+                desc[f"{l1},{l2}"] = d
+                out[f"natgrad{k}_{l1}_{l2}"] = st
+    out["meta"] = np.frombuffer(json.dumps(desc).encode(), dtype=np.uint8)
+    path = os.path.join(HERE, f"tv_{name}_natgrad.npz")
+    np.savez_compressed(path, **out)
+    print(f"tv_{name}: natural gradient for {len(runs)} settings, {os.path.getsize(path)} bytes")
+
+
 if __name__ == "__main__":
     sys.path.insert(0, HERE)
     both = "--ops" not in sys.argv and "--tv" not in sys.argv
@@ -252,3 +297,4 @@ if __name__ == "__main__":
         run_tv_case("3x3_D1_T4_dc16", 3, 3, 1, 4, 16, 515, [61, 62], 3, 6, save_lattice=True)
         run_tv_case("4x4_D2_T8_dc2", 4, 4, 2, 8, 2, 616, [71, 72], 3, 6)
         run_tv_case("3x4_D2_T5_dc3", 3, 4, 2, 5, 3, 717, [81, 82], 3, 6, save_lattice=True)
+        run_tv_natural("4x4_D2_T8_dc2", 4, 4, 2, 8, 2, 616, [71, 72], 3, 6, [(6, 0.0), (50, 1e-3)])

@@ -163,3 +163,28 @@ def test_order_inversions_is_the_leg_reordering_sign():
         conf = (rng.random((3, 4)) < 0.5).astype(int)
         s = fp.order_sign(conf, fp.canonical_names(3, 4, fp.COL), fp.canonical_names(3, 4, fp.ROW), -int(conf.sum()))
         assert s == (-1.0)**fp.order_inversions(conf)
+
+
+def test_natural_gradient_matches_reference():
+    """observer.py:576-675 on the bosonic rows, folded like the gradient, against the reference's
+    natural gradient (4x4, cut 2) for a fixed step count and for an error-bounded run."""
+    z, meta, sites, _ = _load("4x4_D2_T8_dc2")
+    ng = np.load(os.path.join(GOLDEN, "tv_4x4_D2_T8_dc2_natgrad.npz"))
+    ng_meta = json.loads(bytes(ng["meta"]).decode())
+
+    def mk(desc, st):
+        return FermiTensor(desc["names"], [([tuple(x) for x in segs], a) for segs, a in desc["edges"]]).set_storage(st)
+
+    lat = fp.BosonizedLattice(sites, meta["cut"])
+    samples = [(np.asarray(c), z["ws"][i]**2 / z["possibility"][i], z["eloc"][i]) for i, c in enumerate(z["confs"])]
+    for k, (steps, error) in enumerate(ng["runs"]):
+        mine = fp.natural_gradient(lat, samples, int(steps), float(error))
+        refs = []
+        for a in range(4):
+            for b in range(4):
+                ref = mk(ng_meta[f"{a},{b}"], ng[f"natgrad{k}_{a}_{b}"])
+                legs = [x for x in ["T", "U", "D", "L", "R"] if x in ref.names]
+                refs.append((a, b, ref.transpose(["P0"] + legs).data.reshape(mine[a][b].shape)))
+        scale = max(np.abs(r).max() for _, _, r in refs)
+        for a, b, r in refs:
+            assert np.abs(mine[a][b] - r).max() <= 1e-12 * scale, (k, a, b)
