@@ -549,3 +549,54 @@ def natural_gradient(lattice, samples, step, error):
             row.append(g)
         out.append(row)
     return out
+
+
+class FermionSweepChain:
+    """One chain of ``SweepSampling`` (sampling.py:117-154) on a fermionic lattice: the reference's
+    proposal order, RNG draws and acceptance |psi(s')/psi(s)|^2 n/n', with amplitudes from the
+    bosonized row / column strips (a boundary depends only on the rows or columns it covers, so
+    fresh environments after an accepted hop equal the reference's lazily kept ones)."""
+
+    def __init__(self, lattice, terms, conf, seed):
+        from .peps_oracle import sweep_order
+        from .rng import MT19937_64
+        self.lattice = lattice
+        self.conf = np.array(conf, dtype=np.int64)
+        self.engine = MT19937_64(seed)
+        self.terms = []
+        for positions, H in terms:
+            table = {}
+            for key_in, outs in element_table(H).items():
+                table[tuple(s for s, _ in key_in)] = [(tuple(s for s, _ in key_out), float(e.data.reshape(-1)[0]))
+                                                      for key_out, e in outs.items()]
+            self.terms.append((positions, table))
+
+        class _Order:
+            pass
+        shape = _Order()
+        shape.terms, shape.L1, shape.L2 = self.terms, lattice.L1, lattice.L2
+        self.order = sweep_order(shape)
+
+    def sweep(self):
+        from .rng import uniform_int, uniform_real01
+        lat = self.lattice
+        envs = lat.environments(self.conf)
+        ws = float(lat.amplitude(envs).data.reshape(-1)[0])
+        for ti in self.order:
+            positions, table = self.terms[ti]
+            s = tuple(int(self.conf[p[0], p[1]]) for p in positions)
+            if s not in table or not table[s]:
+                continue
+            hops = table[s]
+            n = len(hops)
+            s_new = hops[uniform_int(self.engine, 0, n - 1)][0]
+            n_new = len(table[s_new])
+            wss = float(lat.replace(envs, [p[:2] for p in positions], list(s_new)).data.reshape(-1)[0])
+            p = abs(wss / ws)**2 * n / n_new
+            if uniform_real01(self.engine) < p:
+                ws = wss
+                if s_new != s:
+                    for pos, v in zip(positions, s_new):
+                        self.conf[pos[0], pos[1]] = v
+                    envs = lat.environments(self.conf)
+        return abs(ws)**2, self.conf.copy()

@@ -188,3 +188,23 @@ def test_natural_gradient_matches_reference():
         scale = max(np.abs(r).max() for _, _, r in refs)
         for a, b, r in refs:
             assert np.abs(mine[a][b] - r).max() <= 1e-12 * scale, (k, a, b)
+
+
+@pytest.mark.parametrize("name", ["3x3_D1_T4_dc16", "4x4_D2_T8_dc2", "3x4_D2_T5_dc3"])
+def test_sweep_chains_reproduce_the_reference(name):
+    """The reference's own chains (seeded engines, thermalisation, proposals, acceptance) replayed on
+    the bosonized amplitudes: configurations bit-exact, sampling weights to 1e-12."""
+    z, meta, sites, terms = _load(name)
+    lat = fp.BosonizedLattice(sites, meta["cut"])
+    start = np.array(meta["start"])
+    k = 0
+    for seed in meta["chain_seeds"]:
+        chain = fp.FermionSweepChain(lat, terms, start, seed)
+        for step in range(meta["n_therm"] + meta["n_samples"]):
+            poss, conf = chain.sweep()
+            if step < meta["n_therm"]:
+                continue
+            np.testing.assert_array_equal(conf, z["confs"][k])
+            assert poss == pytest.approx(z["possibility"][k], rel=1e-12, abs=0)
+            k += 1
+    assert k == len(z["confs"])
