@@ -92,3 +92,114 @@ def test_single_process_reduction_is_identity():
     (b,) = allreduce_sum([a])
     assert (a == b).all()
     assert default_seeds(2, 7).tolist() == [7, 8]
+
+
+def _natgrad_data():
+    import numpy as np
+    rng = np.random.default_rng(17)
+    rows = rng.normal(size=(10, 7))
+    w = rng.random(10) + 0.1
+    e = rng.normal(size=10)
+    return rows, w, e
+
+
+def _natgrad_single(rows, w, e, step, error):
+    """The reference's conjugate gradient (observer.py:576-675) over all samples in one process."""
+    import numpy as np
+    W = w.sum()
+    E = (w * e).sum() / W
+    delta = (w[:, None] * rows).sum(axis=0) / W
+    param = np.sqrt(w / W)
+    Dm = (rows - delta) * param[:, None]
+    En = (e - E) * param
+    b = Dm.T @ En
+    x = np.zeros_like(b)
+    r = b - Dm.T @ (Dm @ x)
+    p, rr, t = r, r @ r, 0
+    while t != step and not (error != 0.0 and error**2 > rr / (b @ b)):
+        Dp = Dm @ p
+        alpha = rr / (Dp @ Dp)
+        x = x + alpha * p
+        r = r - alpha * (Dm.T @ Dp)
+        new = r @ r
+        p = r + (new / rr) * p
+        rr = new
+        t += 1
+    return 2 * x
+
+
+class _FakeEngine:
+    """The engine calls the Observer makes, over this rank's hole rows held in host memory."""
+
+    def __init__(self, rows, w, e):
+        import numpy as np
+        self.rows, self.w, self.e = rows, w, e
+        self.np = np
+
+    def keep_holes(self, enable=True):
+        pass
+
+    def reset_observer(self):
+        pass
+
+    def read_observer(self, with_gradient=True):
+        np = self.np
+        scalars = np.array([len(self.w), self.w.sum(), (self.w**2).sum(), 0.0, (self.w * self.e).sum(), 0.0, 0.0, 0.0])
+        delta = (self.w[:, None] * self.rows).sum(axis=0)
+        edelta = ((self.w * self.e)[:, None] * self.rows).sum(axis=0)
+        return scalars, delta, edelta
+
+    def holes_gemv(self, x, transpose=False):
+        return self.rows.T @ x if transpose else self.rows @ x
+
+
+class _FakeOwner:
+    site_number = 1
+    _active_observer = None
+
+    def unflatten(self, flat):
+        return flat
+
+
+def _natgrad_worker(rank, world, port, q):
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from tnsp_gb300.sampling import Observer
+    from test_multirank import _FakeEngine, _FakeOwner, _natgrad_data
+    rows, w, e = _natgrad_data()
+    mine = slice(rank, None, world)
+    out = []
+    for step, error in [(3, 0.0), (50, 1e-6)]:
+        obs = Observer(_FakeOwner(), enable_natural_gradient=True)
+        obs.__enter__()
+        obs._bind(_FakeEngine(rows[mine], w[mine], e[mine]))
+        obs._samples_w = w[mine].tolist()
+        obs._samples_e = e[mine].tolist()
+        obs.__exit__(None, None, None)
+        out.append(obs.natural_gradient_by_conjugate_gradient(step, error).tolist())
+    q.put((rank, out))
+    dist.destroy_process_group()
+
+
+def test_two_rank_natural_gradient_equals_one_process():
+    """Samples split over two gloo ranks: the drop-in Observer's conjugate gradient (its D^T u and
+    |Dp|^2 summed over the ranks) gives the one-process solution over all samples."""
+    import numpy as np
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_natgrad_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    rows, w, e = _natgrad_data()
+    for k, (step, error) in enumerate([(3, 0.0), (50, 1e-6)]):
+        want = _natgrad_single(rows, w, e, step, error)
+        for rank, results in out:
+            np.testing.assert_allclose(results[k], want, rtol=1e-10, atol=1e-12)
