@@ -206,3 +206,31 @@ def test_host_tables_reproduce_the_reference_through_a_dense_sampler(name):
             scale = max(scale, np.abs(ref.storage()).max())
             errs.append(np.abs(diff).max())
     assert max(errs) <= 1e-12 * scale
+
+
+def test_fermionic_workload_layout():
+    """The 8x8 t-V workload: 32 particles, sectors {Q-1:2, Q:4, Q+1:2} on R bonds and column-0 D bonds
+    with tetraku's charge flow Q, {-1:2, 0:4, +1:2} on interior D bonds, U/L legs the conjugates."""
+    lat = F.random_tv(8, 8, (2, 4, 2), 32, seed=3, interior=[(-1, 2), (0, 4), (1, 2)])
+    assert lat.particles == 32 and lat.names[0][0] == ["P0", "T", "D", "R"]
+    e00 = dict(zip(lat.names[0][0], lat.edges[0][0]))
+    assert e00["T"] == ([(-32, 1)], False)
+    assert e00["D"] == ([(27, 2), (28, 4), (29, 2)], False)   # Q = int(32 * 7 / 8)
+    assert e00["R"] == ([(2, 2), (3, 4), (4, 2)], False)      # Q = int(4 * 7 / 8)
+    e33 = dict(zip(lat.names[3][3], lat.edges[3][3]))
+    assert e33["D"] == ([(-1, 2), (0, 4), (1, 2)], False)
+    assert e33["U"] == ([(1, 2), (0, 4), (-1, 2)], True)
+    assert e33["L"] == ([(-1, 2), (-2, 4), (-3, 2)], True)
+    for a in range(8):
+        for b in range(8):
+            t = lat.tensors[a][b]
+            assert t.shape == (2,) + tuple(len(lat.legs[a][b][x]) for x in F.LEGS)
+    # every element outside the charge-conserving blocks is zero
+    for a in range(8):
+        for b in range(8):
+            q = lat.legs[a][b]
+            flux = lat.flux()[a][b]
+            tot = (np.arange(2)[:, None, None, None, None] + np.array(q["U"])[None, :, None, None, None] +
+                   np.array(q["D"])[None, None, :, None, None] + np.array(q["L"])[None, None, None, :, None] +
+                   np.array(q["R"])[None, None, None, None, :])
+            assert not lat.tensors[a][b][tot != flux].any()

@@ -231,23 +231,26 @@ def from_reference_lattice(ref):
 
 def random_tv(L1, L2, D, particles, seed, interior=None, t=1.0, V=1.0, scale=True):
     """A t-V lattice with tetraku's bond layout (tV/__init__.py:52-76): R bonds and the column-0 D
-    bonds carry sectors {Q-1, Q, Q+1} x D with the charge flow Q of those lines, interior D bonds
-    ``interior`` (default tetraku's [(0, D)]); blocks i.i.d. N(0, 1) from numpy's generator, scaled
-    by 1/sqrt(2 D_bond^z) when ``scale``."""
+    bonds carry sectors {Q-1, Q, Q+1} with the charge flow Q of those lines and dimensions ``D`` (an
+    int for all three, or a (d_-, d_0, d_+) triple), interior D bonds ``interior`` (default tetraku's
+    [(0, D)]); blocks i.i.d. N(0, 1) from numpy's generator, scaled by 1/sqrt(2 D_bond^z) when
+    ``scale``.  The 8x8 fermionic workload is ``random_tv(8, 8, (2, 4, 2), 32, seed,
+    interior=[(-1, 2), (0, 4), (1, 2)])``."""
     rng = np.random.default_rng(seed)
     T = particles
+    dims = (D, D, D) if np.isscalar(D) else tuple(D)
     bonds_d = {}
     for l1 in range(L1 - 1):
         Q = int(T * (L1 - l1 - 1) / L1)
-        bonds_d[l1, 0] = [(Q - 1, D), (Q, D), (Q + 1, D)]
+        bonds_d[l1, 0] = [(Q - 1, dims[0]), (Q, dims[1]), (Q + 1, dims[2])]
         for l2 in range(1, L2):
-            bonds_d[l1, l2] = list(interior) if interior is not None else [(0, D)]
+            bonds_d[l1, l2] = list(interior) if interior is not None else [(0, dims[1] if len(set(dims)) > 1 else D)]
     bonds_r = {}
     tt = T / L1
     for l1 in range(L1):
         for l2 in range(L2 - 1):
             Q = int(tt * (L2 - l2 - 1) / L2)
-            bonds_r[l1, l2] = [(Q - 1, D), (Q, D), (Q + 1, D)]
+            bonds_r[l1, l2] = [(Q - 1, dims[0]), (Q, dims[1]), (Q + 1, dims[2])]
     tensors = [[None] * L2 for _ in range(L1)]
     legs = [[None] * L2 for _ in range(L1)]
     edges = [[None] * L2 for _ in range(L1)]
