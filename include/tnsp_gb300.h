@@ -78,6 +78,21 @@ int tnsp_lattice_upload(tnsp_ctx* ctx, int L1, int L2, int P, const int* dims, c
 int tnsp_lattice_charges(tnsp_ctx* ctx, const int* leg_charges, const int* phys_charges, const int* site_flux);
 
 /*
+ * Makes the uploaded lattice fermionic (Fermi U(1), spinless: physical slices 0 = empty, 1 = occupied;
+ * call after tnsp_lattice_upload with P = 2 and tnsp_lattice_charges; a new upload makes it bosonic
+ * again).  slices holds per site, in site order, 8 arrays shaped like the site's (u, d, l, r) slice:
+ * [family][n][prefix parity], family 0 read by the row boundaries and strips, 1 by the column ones,
+ * each the stored slice of occupation n times its static sign and, for prefix parity 1, the parity of
+ * its D (row) or R (column) index.  total_charge is the charge of the T leg of site (0, 0).  The
+ * sampler then evaluates the reference's graded amplitudes: E_loc terms carry the hop's sign (and on
+ * column strips the configuration signs), holes the prefix parity; gradient and natural-gradient rows
+ * stay in the two-slice layout of the upload and take the static per-element sign on the host.
+ * Replaces: TAT's fermionic edge operations and contraction signs (TAT/include/TAT/implement/
+ * edge_operator.hpp:497-612, contract.hpp:381-580, conjugate.hpp:30-122) on this path.
+ */
+int tnsp_lattice_fermion(tnsp_ctx* ctx, const double* slices, int total_charge);
+
+/*
  * Uploads the Hamiltonian: n_terms two-site terms in the reference's dictionary order.
  * sites[t*4 + {0,1,2,3}] = (l1, l2) of positions[0] then positions[1] of term t (nearest
  * neighbours).  For term t and input pair index i = s0*P + s1 (s0 at positions[0]) the outputs

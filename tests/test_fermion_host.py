@@ -234,3 +234,30 @@ def test_fermionic_workload_layout():
                    np.array(q["D"])[None, None, :, None, None] + np.array(q["L"])[None, None, None, :, None] +
                    np.array(q["R"])[None, None, None, None, :])
             assert not lat.tensors[a][b][tot != flux].any()
+
+
+def test_sampler_inputs_of_a_fermionic_lattice():
+    """What engine.Sampler uploads for a fermionic lattice: the dense tensors with U(1) charges and the
+    element tables (tnsp_lattice_upload / _charges / tnsp_model_upload), then every site's eight
+    slices in site order (tnsp_lattice_fermion); the drop-in Observer folds flat gradients."""
+    fl = F.random_tv(3, 4, 2, 5, seed=9)
+    lat = fl.sampling_lattice()
+    assert lat.fermion is fl and lat.P == 2
+    q, qp, flux = lat.charge_arrays()
+    assert qp.tolist() == [0, 1] and flux.reshape(3, 4)[0, 0] == 5 and not flux.reshape(3, 4)[1:].any()
+    flat = fl.slices_flat()
+    assert flat.size == 8 * sum(t[0].size for row in fl.tensors for t in row)
+    pos = 0
+    for a in range(3):
+        for b in range(4):
+            sl = fl.sign_folded_slices(a, b)
+            np.testing.assert_array_equal(flat[pos:pos + sl.size], sl.ravel())
+            pos += sl.size
+    g = np.arange(lat.flat_tensors().size, dtype=np.float64)
+    folded = lat.unflatten(fl.fold_flat(g))
+    raw = lat.unflatten(g)
+    for a in range(3):
+        for b in range(4):
+            np.testing.assert_array_equal(folded[a][b], fl.fold_gradient(a, b, raw[a][b]))
+    n, sites, offs, cnts, outs, vals = lat.term_arrays()
+    assert n == len(fl.terms) == 3 * 3 + 2 * 4

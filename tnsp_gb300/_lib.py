@@ -43,6 +43,7 @@ SIGNATURES = {
     "tnsp_lattice_upload": (ctypes.c_int,
                             [_c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_int_p, _c_dbl_p, ctypes.c_int]),
     "tnsp_lattice_charges": (ctypes.c_int, [_c_void_p, _c_int_p, _c_int_p, _c_int_p]),
+    "tnsp_lattice_fermion": (ctypes.c_int, [_c_void_p, _c_dbl_p, ctypes.c_int]),
     "tnsp_model_upload": (ctypes.c_int,
                           [_c_void_p, ctypes.c_int, _c_int_p, _c_int_p, _c_int_p, ctypes.c_int, _c_int_p, _c_dbl_p]),
     "tnsp_chains_init": (ctypes.c_int, [_c_void_p, ctypes.c_int, _c_i32_p, _c_u64_p, ctypes.c_int, ctypes.c_int]),

@@ -29,6 +29,13 @@ struct tnsp_ctx {
   int* d_qphys = nullptr;          // [P]
   int* d_sflux = nullptr;          // [site]
   bool charged = false;
+  // fermionic lattice (tnsp_lattice_fermion): eight sign-folded slices per site and their offsets
+  bool fermion = false;
+  int fermion_pT = 0;
+  double* dF64 = nullptr;
+  float* dF32 = nullptr;
+  tnsp::dd* dFdd = nullptr;
+  long long* d_foff = nullptr;
   // model
   int n_terms = 0;
   int* d_term_sites = nullptr;

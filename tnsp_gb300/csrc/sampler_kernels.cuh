@@ -59,6 +59,12 @@ struct Model {
   const int* qleg;          // [site][4][Dmax]: charge of each index of the U, D, L, R legs
   const int* qphys;         // [P]
   const int* sflux;         // [site]
+  // fermionic lattice: A holds eight slices per site, [family][n][prefix parity][u][d][l][r] (family 0
+  // for the row orientations, 1 for the column ones), and the gradient accumulators / hole rows use
+  // the two-slice parameter layout at poff (null: the layout of off)
+  int fermion;
+  int pT;                   // parity of the T leg's charge
+  const long long* poff;
 };
 
 struct Chains {
@@ -198,13 +204,16 @@ template <class T> struct Chain {
 
   // site (l1, l2) at physical index s in one of four orientations:
   //   0: (U, D, L, R)   1: (D, U, L, R)   2: (L, R, U, D)   3: (R, L, U, D)
-  __device__ SiteView site(int l1, int l2, int s, int orient) const {
+  //   fermionic lattices: ``mp`` is the number of particles before the site along its row (orientations
+  //   0, 1) or column (2, 3) in the configuration being evaluated; its parity picks the slice
+  __device__ SiteView site(int l1, int l2, int s, int orient, int mp = 0) const {
     const int id = l1 * md.L2 + l2;
     const int* d = md.dims + id * 4;
     const int U = d[0], D = d[1], L = d[2], R = d[3];
     const int sR = 1, sL = R, sD = L * R, sU = D * L * R;
     SiteView v;
-    v.base = md.off[id] + (long long)s * U * D * L * R;
+    const long long slice = md.fermion ? ((long long)((orient >= 2 ? 2 : 0) + s) * 2 + (mp & 1)) : (long long)s;
+    v.base = md.off[id] + slice * U * D * L * R;
     const int* q = md.qleg + (long long)id * 4 * md.Dmax;
     const int *qU = q, *qD = q + md.Dmax, *qL = q + 2 * md.Dmax, *qR = q + 3 * md.Dmax;
     v.flux = md.sflux[id] - md.qphys[s];
@@ -540,9 +549,11 @@ template <class T> struct Engine : Chain<T> {
     __syncthreads();
     int expo = lexpo(f, prev);
     long long t0 = tic();
+    int prefix = 0;
     for (int i = 0; i < n; ++i) {
       const int l1 = (f < 2) ? idx : i, l2 = (f < 2) ? i : idx;
-      const SiteView w = site(l1, l2, conf[l1 * md.L2 + l2], orient);
+      const SiteView w = site(l1, l2, conf[l1 * md.L2 + l2], orient, prefix);
+      prefix += conf[l1 * md.L2 + l2];
       const Dims3 ld = lsdim(f, prev, i);
       two_line(lsite(f, prev, i), ld, A, w, Tbuf(s_buf[i]));
       this->count(0, 2.0 * ld.a * w.dl * w.dd * ld.b * w.dr * ld.p);
@@ -1050,11 +1061,11 @@ template <class T> struct Engine : Chain<T> {
   }
 
   // E[c+1] = E[c] x column c (physical index s); writes into dst with exponent returned
-  __device__ int step_left(int kind, int idx, int c, const T* Ein, Dims3 e, int s, T* dst) {
+  __device__ int step_left(int kind, int idx, int c, const T* Ein, Dims3 e, int s, T* dst, int mp = 0) {
     const long long t0 = tic();
     int l1, l2;
     strip_site_rc(kind, idx, c, l1, l2);
-    const SiteView w = site(l1, l2, s, kind == 0 ? 0 : 2);
+    const SiteView w = site(l1, l2, s, kind == 0 ? 0 : 2, mp);
     strip_left(Ein, e.a, e.p, e.b, lsite(fup(kind), idx - 1, c), lsdim(fup(kind), idx - 1, c), A, w,
                lsite(fdn(kind), idx + 1, c), lsdim(fdn(kind), idx + 1, c), slot + sl.o_t1, slot + sl.o_t2, dst);
     const Dims3 up = lsdim(fup(kind), idx - 1, c), dn = lsdim(fdn(kind), idx + 1, c);
@@ -1064,11 +1075,11 @@ template <class T> struct Engine : Chain<T> {
     toc(PH_STRIP, t0);
     return ex;
   }
-  __device__ int step_right(int kind, int idx, int c, const T* Fin, Dims3 f, int s, T* dst) {
+  __device__ int step_right(int kind, int idx, int c, const T* Fin, Dims3 f, int s, T* dst, int mp = 0) {
     const long long t0 = tic();
     int l1, l2;
     strip_site_rc(kind, idx, c, l1, l2);
-    const SiteView w = site(l1, l2, s, kind == 0 ? 0 : 2);
+    const SiteView w = site(l1, l2, s, kind == 0 ? 0 : 2, mp);
     strip_right(Fin, f.a, f.p, f.b, lsite(fup(kind), idx - 1, c), lsdim(fup(kind), idx - 1, c), A, w,
                 lsite(fdn(kind), idx + 1, c), lsdim(fdn(kind), idx + 1, c), slot + sl.o_t1, slot + sl.o_t2, dst);
     const Dims3 up = lsdim(fup(kind), idx - 1, c), dn = lsdim(fdn(kind), idx + 1, c);
@@ -1083,6 +1094,14 @@ template <class T> struct Engine : Chain<T> {
     int l1, l2;
     strip_site_rc(kind, idx, c, l1, l2);
     return conf[l1 * md.L2 + l2];
+  }
+
+  // particles at strip positions before c (0 for a bosonic lattice, where it is not used)
+  __device__ int strip_prefix(int kind, int idx, int c) const {
+    int n = 0;
+    if (md.fermion)
+      for (int k = 0; k < c; ++k) n += conf_at(kind, idx, k);
+    return n;
   }
 
   // build the strip (kind, idx) for the current configuration: all F, E[0]
@@ -1100,7 +1119,8 @@ template <class T> struct Engine : Chain<T> {
     }
     __syncthreads();
     for (int c = n - 1; c >= 0; --c) {
-      const int e = step_right(kind, idx, c, Fbuf(c + 1), Fdims(kind, idx, c + 1), conf_at(kind, idx, c), Fbuf(c));
+      const int e = step_right(kind, idx, c, Fbuf(c + 1), Fdims(kind, idx, c + 1), conf_at(kind, idx, c), Fbuf(c),
+                               strip_prefix(kind, idx, c));
       if (threadIdx.x == 0) eF[c] = eF[c + 1] + e;
       __syncthreads();
     }
@@ -1117,7 +1137,8 @@ template <class T> struct Engine : Chain<T> {
     // make E[c] valid
     while (*strip_eupto < c) {
       const int k = *strip_eupto;
-      const int e = step_left(kind, idx, k, Ebuf(k), Edims(kind, idx, k), conf_at(kind, idx, k), Ebuf(k + 1));
+      const int e = step_left(kind, idx, k, Ebuf(k), Edims(kind, idx, k), conf_at(kind, idx, k), Ebuf(k + 1),
+                              strip_prefix(kind, idx, k));
       if (threadIdx.x == 0) {
         eE[k + 1] = eE[k] + e;
         *strip_eupto = k + 1;
@@ -1130,8 +1151,9 @@ template <class T> struct Engine : Chain<T> {
   __device__ void strip_replace2(int kind, int idx, int c, int s0, int s1, double& m, int& ex) {
     T* w0 = slot + sl.o_w0;
     T* w1 = slot + sl.o_w1;
-    const int e0 = step_left(kind, idx, c, Ebuf(c), Edims(kind, idx, c), s0, w0);
-    const int e1 = step_left(kind, idx, c + 1, w0, Edims(kind, idx, c + 1), s1, w1);
+    const int mp0 = strip_prefix(kind, idx, c);  // the pair's second site counts the first one's new value
+    const int e0 = step_left(kind, idx, c, Ebuf(c), Edims(kind, idx, c), s0, w0, mp0);
+    const int e1 = step_left(kind, idx, c + 1, w0, Edims(kind, idx, c + 1), s1, w1, mp0 + s0);
     const Dims3 fd = Fdims(kind, idx, c + 2);
     const T v = block_dot(w1, Fbuf(c + 2), (long long)fd.a * fd.p * fd.b, red);
     m = (double)v;
@@ -1149,7 +1171,7 @@ template <class T> struct Engine : Chain<T> {
     int e = 0;
     Dims3 fd{1, 1, 1};
     for (int c = n - 1; c >= 0; --c) {
-      e += step_right(0, 0, c, f0, fd, conf_at(0, 0, c), f1);
+      e += step_right(0, 0, c, f0, fd, conf_at(0, 0, c), f1, strip_prefix(0, 0, c));
       fd = Fdims(0, 0, c);
       T* t = f0;
       f0 = f1;
@@ -1175,6 +1197,53 @@ template <class T> __device__ void bind_slot(Engine<T>& eng, const Slots& sl, co
 
 __device__ __forceinline__ double ratio_of(double m1, int e1, double m0, int e0) {
   return ldexp(m1 / m0, e1 - e0);
+}
+
+// occupation of site i of a fermionic configuration with sites ia, ib replaced by na, nb
+__device__ __forceinline__ int occ_after(const short* conf, int i, int ia, int na, int ib, int nb) {
+  return i == ia ? na : i == ib ? nb : conf[i];
+}
+
+// parity bit of the configuration sign prod_k (-1)^((N_<k + p_T)(N_<=k + p_T)) over the cuts between rows
+// (rows = 1) or columns (rows = 0), of the configuration with sites ia, ib replaced
+__device__ inline int config_sign_bit(const short* conf, int L1, int L2, int pT, int rows, int ia, int na, int ib, int nb) {
+  const int nk = rows ? L1 : L2, len = rows ? L2 : L1;
+  int s = 0, before = pT & 1;
+  for (int k = 0; k + 1 < nk; ++k) {
+    int cnt = 0;
+    for (int j = 0; j < len; ++j) cnt += occ_after(conf, rows ? k * L2 + j : j * L2 + k, ia, na, ib, nb);
+    const int upto = (before + cnt) & 1;
+    s ^= before & upto;
+    before = upto;
+  }
+  return s;
+}
+
+// sign of one E_loc term of a fermionic lattice, for amplitudes ws from the row strips and wss from the
+// row (horizontal pair) or column (vertical pair) strips of the bosonized slices: the hop's string of
+// particles between the two sites in row-major order (-1 more for a forward move) and, for a vertical
+// pair, the column and row configuration signs and the parity of the order inversions of the new
+// configuration
+__device__ inline double fermion_term_sign(const short* conf, int L1, int L2, int pT, int ia, int na, int ib, int nb,
+                                    int vertical) {
+  const int i = ia < ib ? ia : ib, j = ia < ib ? ib : ia;
+  const int new_i = i == ia ? na : nb;
+  int s = 0;
+  for (int k = i + 1; k < j; ++k) s ^= conf[k] & 1;
+  if (conf[i] == 1 && new_i == 0) s ^= 1;
+  if (vertical) {
+    s ^= config_sign_bit(conf, L1, L2, pT, 0, ia, na, ib, nb);
+    s ^= config_sign_bit(conf, L1, L2, pT, 1, -1, 0, -1, 0);
+    int inv = 0;
+    for (int a = 1; a < L1; ++a)
+      for (int b = 0; b + 1 < L2; ++b) {
+        if (!occ_after(conf, a * L2 + b, ia, na, ib, nb)) continue;
+        for (int a2 = 0; a2 < a; ++a2)
+          for (int b2 = b + 1; b2 < L2; ++b2) inv += occ_after(conf, a2 * L2 + b2, ia, na, ib, nb);
+      }
+    s ^= inv & 1;
+  }
+  return s ? -1.0 : 1.0;
 }
 
 // one Metropolis proposal on the term at (kind, idx, c)-(kind, idx, c+1)
@@ -1390,7 +1459,10 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Sl
                 double m;
                 int e;
                 eng.strip_replace2(kind, idx, c, na, nb, m, e);
-                if (m != 0.0) total += v * ratio_of(m, e, ws_m, ws_e);
+                const double sg = md.fermion ? fermion_term_sign(s_conf, md.L1, md.L2, md.pT, l1a * md.L2 + l2a, na,
+                                                                 l1b * md.L2 + l2b, nb, kind)
+                                             : 1.0;
+                if (m != 0.0) total += sg * v * ratio_of(m, e, ws_m, ws_e);
               } else {
                 if (threadIdx.x == 0) atomicOr(ch.status, ST_UNSUPPORTED);
               }
@@ -1433,15 +1505,24 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Sl
             const int id = l1 * md.L2 + l2;
             const int* d = md.dims + id * 4;
             const long long n = (long long)d[0] * d[1] * d[2] * d[3];
-            const long long base = md.off[id] + (long long)s_conf[id] * n;
+            const long long base = (md.poff ? md.poff : md.off)[id] + (long long)s_conf[id] * n;
+            // fermionic lattice: the hole of a slice read with an odd row prefix carries the prefix parity
+            // on its odd D indices
+            const int* qD = md.qleg + (long long)id * 4 * md.Dmax + md.Dmax;
+            const int LR = d[2] * d[3];
+            const bool odd_prefix = md.fermion && (eng.strip_prefix(0, l1, l2) & 1);
             for (long long q = threadIdx.x; q < n; q += blockDim.x) {
-              const double hv = (double)h[q] * f;
+              double hv = (double)h[q] * f;
+              if (odd_prefix && (qD[(q / LR) % d[1]] & 1)) hv = -hv;
               delta[base + q] += hv;
               edelta[base + q] += eloc * hv;
             }
             if (ch.rec_hole) {
               double* row = ch.rec_hole + (ch.hole_row0 + (long long)(rec_base + sw) * ch.B + b) * md.n_params;
-              for (long long q = threadIdx.x; q < n; q += blockDim.x) row[base + q] = (double)h[q] * fh;
+              for (long long q = threadIdx.x; q < n; q += blockDim.x) {
+                const double hv = (double)h[q] * fh;
+                row[base + q] = (odd_prefix && (qD[(q / LR) % d[1]] & 1)) ? -hv : hv;
+              }
             }
             __syncthreads();
           }

@@ -139,7 +139,16 @@ void free_model(tnsp_ctx* c) {
   c->has_model = false;
 }
 
+void free_fermion(tnsp_ctx* c) {
+  dfree(c->dF64);
+  dfree(c->dF32);
+  dfree(c->dFdd);
+  dfree(c->d_foff);
+  c->fermion = false;
+}
+
 void free_lattice(tnsp_ctx* c) {
+  free_fermion(c);
   dfree(c->dA64);
   dfree(c->dA32);
   dfree(c->dAdd);
@@ -163,6 +172,15 @@ Model make_model(tnsp_ctx* c) {
   m.A = c->precision == TNSP_FP64 ? (const void*)c->dA64
         : c->precision == TNSP_DD  ? (const void*)c->dAdd
                                    : (const void*)c->dA32;
+  if (c->fermion) {
+    m.fermion = 1;
+    m.pT = c->fermion_pT;
+    m.poff = c->d_off;
+    m.off = c->d_foff;
+    m.A = c->precision == TNSP_FP64 ? (const void*)c->dF64
+          : c->precision == TNSP_DD  ? (const void*)c->dFdd
+                                     : (const void*)c->dF32;
+  }
   m.n_terms = c->n_terms;
   m.term_sites = c->d_term_sites;
   m.hterm = c->d_hterm;
@@ -374,6 +392,7 @@ int tnsp_lattice_upload(tnsp_ctx* ctx, int L1, int L2, int P, const int* dims, c
     free_chains(ctx);
     free_model(ctx);
   }
+  free_fermion(ctx);  // a new upload describes a bosonic lattice until tnsp_lattice_fermion is called again
   if (!ctx->has_lattice || reshape) {
     free_lattice(ctx);
     CK(cudaMalloc((void**)&ctx->dA64, sizeof(double) * total));
@@ -454,6 +473,39 @@ int tnsp_lattice_charges(tnsp_ctx* ctx, const int* leg_charges, const int* phys_
   CK(cudaMemcpy(ctx->d_qphys, phys_charges, sizeof(int) * P, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_sflux, site_flux, sizeof(int) * (size_t)L1 * L2, cudaMemcpyHostToDevice));
   ctx->charged = true;
+  return TNSP_OK;
+}
+
+int tnsp_lattice_fermion(tnsp_ctx* ctx, const double* slices, int total_charge) {
+  if (!ctx) return TNSP_E_ARG;
+  if (!ctx->has_lattice) return fail(ctx, TNSP_E_STATE, "upload the lattice first");
+  if (!ctx->charged) return fail(ctx, TNSP_E_STATE, "declare the charges first");
+  if (ctx->P != 2) return fail(ctx, TNSP_E_ARG, "a fermionic site has two physical slices (empty, occupied)");
+  if (!slices) return fail(ctx, TNSP_E_ARG, "null slices");
+  CK(cudaSetDevice(ctx->device));
+  const int nsite = ctx->L1 * ctx->L2;
+  std::vector<long long> foff(nsite);
+  long long total = 0;
+  for (int id = 0; id < nsite; ++id) {
+    const int* d = &ctx->dims[id * 4];
+    foff[id] = total;
+    total += 8LL * d[0] * d[1] * d[2] * d[3];
+  }
+  for (long long i = 0; i < total; ++i)
+    if (!std::isfinite(slices[i])) return fail(ctx, TNSP_E_ARG, "non-finite element in the slices");
+  free_fermion(ctx);
+  CK(cudaMalloc((void**)&ctx->dF64, sizeof(double) * total));
+  CK(cudaMalloc((void**)&ctx->dF32, sizeof(float) * total));
+  CK(cudaMalloc((void**)&ctx->dFdd, sizeof(dd) * total));
+  CK(cudaMalloc((void**)&ctx->d_foff, sizeof(long long) * nsite));
+  CK(cudaMemcpyAsync(ctx->dF64, slices, sizeof(double) * total, cudaMemcpyHostToDevice, ctx->stream));
+  convert_tensors<<<(int)std::min<long long>(1024, (total + 255) / 256), 256, 0, ctx->stream>>>(ctx->dF64, total,
+                                                                                               ctx->dF32, ctx->dFdd);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(ctx->d_foff, foff.data(), sizeof(long long) * nsite, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->fermion = true;
+  ctx->fermion_pT = total_charge & 1;
   return TNSP_OK;
 }
 

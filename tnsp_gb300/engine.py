@@ -64,6 +64,13 @@ class Sampler:
             self._check(
                 self.lib.tnsp_lattice_charges(self.ctx, ptr(q, ctypes.c_int), ptr(qp, ctypes.c_int),
                                               ptr(fl, ctypes.c_int)), "tnsp_lattice_charges")
+        fermion = getattr(lat, "fermion", None)
+        if fermion is not None:
+            # a fermionic lattice (tnsp_gb300.fermion): the current tensors as sign-folded slices
+            slices = np.ascontiguousarray(
+                fermion.slices_flat([[lat[l1, l2] for l2 in range(lat.L2)] for l1 in range(lat.L1)]))
+            self._check(self.lib.tnsp_lattice_fermion(self.ctx, ptr(slices, ctypes.c_double), fermion.T_charge),
+                        "tnsp_lattice_fermion")
         if not self._static_uploaded:
             n, sites, offs, cnts, outs, vals = lat.term_arrays()
             self._check(
@@ -167,6 +174,12 @@ class Sampler:
         self._check(
             self.lib.tnsp_amplitude(self.ctx, B, ptr(configs.reshape(B, -1), ctypes.c_int32), ptr(m, ctypes.c_double),
                                     ptr(e, ctypes.c_int32)), "tnsp_amplitude")
+        fermion = getattr(self.lattice, "fermion", None)
+        if fermion is not None:
+            # the graded amplitude in the row-major canonical leg order (T, P_0_0_0, P_0_1_0, ...)
+            from .fermion import ROW, configuration_sign
+            shape = (B, self.lattice.L1, self.lattice.L2)
+            m = m * np.array([configuration_sign(c, fermion.p_T, ROW) for c in configs.reshape(shape)])
         return m, e
 
     def status(self):

@@ -99,9 +99,10 @@ class FermionLattice:
         (U, D, L, R), shape = self._grid(l1, l2)
         return np.where(np.broadcast_to(D if family == ROW else R, shape).astype(bool), -1.0, 1.0)
 
-    def sign_folded_slices(self, l1, l2):
-        """float64 [2 families][2 occupations][2 prefix parities][u][d][l][r]."""
-        a = self.tensors[l1][l2]
+    def sign_folded_slices(self, l1, l2, tensor=None):
+        """float64 [2 families][2 occupations][2 prefix parities][u][d][l][r] of the site's tensor (or of
+        ``tensor``, the same site after a gradient step)."""
+        a = self.tensors[l1][l2] if tensor is None else np.asarray(tensor)
         out = np.empty((2, 2, 2) + a.shape[1:])
         for family in (ROW, COL):
             prefix = self.prefix_sign(l1, l2, family)
@@ -122,6 +123,32 @@ class FermionLattice:
         for n in (0, 1):
             out[n] *= self.gradient_sign(l1, l2, n)
         return out
+
+    def slices_flat(self, tensors=None):
+        """Every site's eight slices, in site order: the array ``tnsp_lattice_fermion`` takes."""
+        return np.concatenate([self.sign_folded_slices(l1, l2, None if tensors is None else tensors[l1][l2]).ravel()
+                               for l1 in range(self.L1) for l2 in range(self.L2)])
+
+    def fold_flat(self, flat):
+        """``fold_gradient`` over the flat (site-ordered, (n, u, d, l, r) per site) parameter vector."""
+        out, pos = [], 0
+        for l1 in range(self.L1):
+            for l2 in range(self.L2):
+                n = self.tensors[l1][l2].size
+                out.append(self.fold_gradient(l1, l2, np.asarray(flat[pos:pos + n]).reshape(self.tensors[l1][l2].shape))
+                           .ravel())
+                pos += n
+        return np.concatenate(out)
+
+    def sampling_lattice(self):
+        """The lattice the sampler takes: dense tensors, the Fermi U(1) charges as U(1) charges, the
+        element tables, and this object as its ``fermion`` attribute, which makes ``engine.Sampler``
+        upload the sign-folded slices and the drop-in Observer fold its gradients."""
+        from .lattice import SamplingLattice
+        lat = SamplingLattice(self.L1, self.L2, 2, [[t.copy() for t in row] for row in self.tensors], dict(self.terms),
+                              self.charges())
+        lat.fermion = self
+        return lat
 
     def to_blocks(self, l1, l2, dense):
         """Block storage (TAT core order, the site's own leg order) of a dense (p, u, d, l, r) array."""

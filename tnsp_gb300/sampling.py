@@ -250,7 +250,12 @@ class Observer:
         if not self._enable_gradient:
             raise RuntimeError("gradient not enabled")
         scal = self._read()
-        return self.owner.unflatten(gradient_from(scal, self._delta, self._edelta))
+        return self.owner.unflatten(self._fold(gradient_from(scal, self._delta, self._edelta)))
+
+    def _fold(self, flat):
+        """A fermionic lattice's gradient takes its static per-element sign (tnsp_gb300.fermion)."""
+        fermion = getattr(self.owner, "fermion", None)
+        return flat if fermion is None else fermion.fold_flat(flat)
 
     def natural_gradient_by_conjugate_gradient(self, step, error):
         """``Observer.natural_gradient_by_conjugate_gradient``
@@ -303,7 +308,7 @@ class Observer:
             p = r + beta * p
             t += 1
         self.natural_gradient_steps = t
-        return self.owner.unflatten(2 * x)
+        return self.owner.unflatten(self._fold(2 * x))
 
     @property
     def instability(self):
