@@ -1200,13 +1200,13 @@ __device__ __forceinline__ double ratio_of(double m1, int e1, double m0, int e0)
 }
 
 // occupation of site i of a fermionic configuration with sites ia, ib replaced by na, nb
-__device__ __forceinline__ int occ_after(const short* conf, int i, int ia, int na, int ib, int nb) {
+__host__ __device__ __forceinline__ int occ_after(const short* conf, int i, int ia, int na, int ib, int nb) {
   return i == ia ? na : i == ib ? nb : conf[i];
 }
 
 // parity bit of the configuration sign prod_k (-1)^((N_<k + p_T)(N_<=k + p_T)) over the cuts between rows
 // (rows = 1) or columns (rows = 0), of the configuration with sites ia, ib replaced
-__device__ inline int config_sign_bit(const short* conf, int L1, int L2, int pT, int rows, int ia, int na, int ib, int nb) {
+__host__ __device__ inline int config_sign_bit(const short* conf, int L1, int L2, int pT, int rows, int ia, int na, int ib, int nb) {
   const int nk = rows ? L1 : L2, len = rows ? L2 : L1;
   int s = 0, before = pT & 1;
   for (int k = 0; k + 1 < nk; ++k) {
@@ -1224,7 +1224,7 @@ __device__ inline int config_sign_bit(const short* conf, int L1, int L2, int pT,
 // particles between the two sites in row-major order (-1 more for a forward move) and, for a vertical
 // pair, the column and row configuration signs and the parity of the order inversions of the new
 // configuration
-__device__ inline double fermion_term_sign(const short* conf, int L1, int L2, int pT, int ia, int na, int ib, int nb,
+__host__ __device__ inline double fermion_term_sign(const short* conf, int L1, int L2, int pT, int ia, int na, int ib, int nb,
                                     int vertical) {
   const int i = ia < ib ? ia : ib, j = ia < ib ? ib : ia;
   const int new_i = i == ia ? na : nb;
