@@ -158,6 +158,20 @@ __device__ inline double draw_uniform_real(uint64_t* mt, int& mti) {
 // ------------------------------------------------------------------------------------------
 // views
 // ------------------------------------------------------------------------------------------
+// which of a fermionic site's eight slices [family][n][prefix parity] a view reads: family 0 for the row
+// orientations (0, 1), 1 for the column ones (2, 3)
+__host__ __device__ __forceinline__ long long fermion_slice(int orient, int s, int mp) {
+  return (long long)((orient >= 2 ? 2 : 0) + s) * 2 + (mp & 1);
+}
+
+// particles before strip position c of line idx: the sites of row idx left of column c (kind 0) or the
+// sites of column idx above row c (kind 1)
+__host__ __device__ inline int strip_prefix_of(const short* conf, int L2, int kind, int idx, int c) {
+  int n = 0;
+  for (int k = 0; k < c; ++k) n += kind == 0 ? conf[idx * L2 + k] : conf[k * L2 + idx];
+  return n;
+}
+
 struct SiteView {  // a projected site tensor seen as W(u, d, l, r)
   long long base;
   int du, dd, dl, dr;
@@ -212,7 +226,7 @@ template <class T> struct Chain {
     const int U = d[0], D = d[1], L = d[2], R = d[3];
     const int sR = 1, sL = R, sD = L * R, sU = D * L * R;
     SiteView v;
-    const long long slice = md.fermion ? ((long long)((orient >= 2 ? 2 : 0) + s) * 2 + (mp & 1)) : (long long)s;
+    const long long slice = md.fermion ? fermion_slice(orient, s, mp) : (long long)s;
     v.base = md.off[id] + slice * U * D * L * R;
     const int* q = md.qleg + (long long)id * 4 * md.Dmax;
     const int *qU = q, *qD = q + md.Dmax, *qL = q + 2 * md.Dmax, *qR = q + 3 * md.Dmax;
@@ -1098,10 +1112,7 @@ template <class T> struct Engine : Chain<T> {
 
   // particles at strip positions before c (0 for a bosonic lattice, where it is not used)
   __device__ int strip_prefix(int kind, int idx, int c) const {
-    int n = 0;
-    if (md.fermion)
-      for (int k = 0; k < c; ++k) n += conf_at(kind, idx, k);
-    return n;
+    return md.fermion ? strip_prefix_of(conf, md.L2, kind, idx, c) : 0;
   }
 
   // build the strip (kind, idx) for the current configuration: all F, E[0]
