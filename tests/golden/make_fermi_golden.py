@@ -150,7 +150,8 @@ def _tensor_record(t):
     return {"names": names, "edges": edges}, np.array(t.storage, dtype=np.float64).copy()
 
 
-def run_tv_case(name, L1, L2, D, T, cut, tensor_seed, chain_seeds, n_therm, n_samples, save_lattice=False):
+def run_tv_case(name, L1, L2, D, T, cut, tensor_seed, chain_seeds, n_therm, n_samples, save_lattice=False,
+                interior=None):
     """Sweep chains of the reference on a t-V lattice (t = V = 1); records per sample the amplitude
     tensor hole(()) and E_loc (observer.py:313-415)."""
     sys.argv = sys.argv[:1] + [a for a in sys.argv[1:] if not a.startswith("--")]
@@ -159,6 +160,11 @@ def run_tv_case(name, L1, L2, D, T, cut, tensor_seed, chain_seeds, n_therm, n_sa
     from tetraku.models import tV
 
     state = tV.abstract_lattice(L1, L2, D, T, 1.0, 1.0)
+    if interior is not None:
+        # interior D bonds with odd charges (the 8x8 workload's {-1, 0, +1} layout, scaled down)
+        for l1 in range(L1 - 1):
+            for l2 in range(1, L2):
+                state.virtual_bond[l1, l2, "D"] = interior
     TAT.random.seed(tensor_seed)
     lattice = tet.SamplingLattice(state)
     for l1 in range(L1):
@@ -298,3 +304,5 @@ if __name__ == "__main__":
         run_tv_case("4x4_D2_T8_dc2", 4, 4, 2, 8, 2, 616, [71, 72], 3, 6)
         run_tv_case("3x4_D2_T5_dc3", 3, 4, 2, 5, 3, 717, [81, 82], 3, 6, save_lattice=True)
         run_tv_natural("4x4_D2_T8_dc2", 4, 4, 2, 8, 2, 616, [71, 72], 3, 6, [(6, 0.0), (50, 1e-3)])
+        run_tv_case("4x4_D1odd_T8_dc3", 4, 4, 1, 8, 3, 818, [91, 92], 3, 6,
+                    interior=[(-1, 1), (0, 2), (1, 1)])

@@ -37,7 +37,7 @@ def test_exact_graded_contraction_matches_reference():
         assert fp.local_energy(sites, terms, conf) == pytest.approx(z["eloc"][i], rel=1e-12, abs=1e-12)
 
 
-@pytest.mark.parametrize("name", ["3x3_D1_T4_dc16", "4x4_D2_T8_dc2", "3x4_D2_T5_dc3"])
+@pytest.mark.parametrize("name", ["3x3_D1_T4_dc16", "4x4_D2_T8_dc2", "3x4_D2_T5_dc3", "4x4_D1odd_T8_dc3"])
 def test_bosonized_boundary_mps_matches_reference(name):
     """The bosonized lattice through the dense oracle reproduces the reference's amplitudes and E_loc,
     including with a cut of 2 where truncation changes the amplitudes by percents."""
@@ -49,7 +49,7 @@ def test_bosonized_boundary_mps_matches_reference(name):
         assert lat.local_energy(terms, conf) == pytest.approx(z["eloc"][i], rel=1e-12, abs=1e-12)
 
 
-@pytest.mark.parametrize("name", ["4x4_D2_T8_dc2", "3x4_D2_T5_dc3"])
+@pytest.mark.parametrize("name", ["4x4_D2_T8_dc2", "3x4_D2_T5_dc3", "4x4_D1odd_T8_dc3"])
 def test_truncation_is_active_in_the_truncated_cases(name):
     z, meta, sites, terms = _load(name)
     rel = [abs(fp.value(fp.amplitude(sites, c), meta["ws_names"][i]) / z["ws"][i] - 1) for i, c in enumerate(z["confs"])]
@@ -126,7 +126,7 @@ def test_exact_graded_holes_match_reference():
                 assert np.abs(mine.data - ref.data).max() <= 1e-12 * np.abs(ref.data).max()
 
 
-@pytest.mark.parametrize("name", ["3x3_D1_T4_dc16", "4x4_D2_T8_dc2", "3x4_D2_T5_dc3"])
+@pytest.mark.parametrize("name", ["3x3_D1_T4_dc16", "4x4_D2_T8_dc2", "3x4_D2_T5_dc3", "4x4_D1odd_T8_dc3"])
 def test_gradient_from_bosonic_holes_matches_reference(name):
     z, meta, sites, _ = _load(name)
 
@@ -147,7 +147,7 @@ def test_gradient_from_bosonic_holes_matches_reference(name):
         assert np.abs(mine[a][b] - r).max() <= 1e-12 * scale, (a, b)
 
 
-@pytest.mark.parametrize("name", ["3x3_D1_T4_dc16", "4x4_D2_T8_dc2", "3x4_D2_T5_dc3"])
+@pytest.mark.parametrize("name", ["3x3_D1_T4_dc16", "4x4_D2_T8_dc2", "3x4_D2_T5_dc3", "4x4_D1odd_T8_dc3"])
 def test_local_energy_from_strip_values_and_integer_signs(name):
     """The form a dense kernel evaluates: strip values of the bosonized lattice times signs computed
     from particle counts alone."""
@@ -190,7 +190,7 @@ def test_natural_gradient_matches_reference():
             assert np.abs(mine[a][b] - r).max() <= 1e-12 * scale, (k, a, b)
 
 
-@pytest.mark.parametrize("name", ["3x3_D1_T4_dc16", "4x4_D2_T8_dc2", "3x4_D2_T5_dc3"])
+@pytest.mark.parametrize("name", ["3x3_D1_T4_dc16", "4x4_D2_T8_dc2", "3x4_D2_T5_dc3", "4x4_D1odd_T8_dc3"])
 def test_sweep_chains_reproduce_the_reference(name):
     """The reference's own chains (seeded engines, thermalisation, proposals, acceptance) replayed on
     the bosonized amplitudes: configurations bit-exact, sampling weights to 1e-12."""

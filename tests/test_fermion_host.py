@@ -168,7 +168,7 @@ class _Emulator:
         return psi * F.configuration_sign(conf, self.h.p_T, F.ROW), eloc, holes
 
 
-@pytest.mark.parametrize("name", ["3x3_D1_T4_dc16", "4x4_D2_T8_dc2", "3x4_D2_T5_dc3"])
+@pytest.mark.parametrize("name", ["3x3_D1_T4_dc16", "4x4_D2_T8_dc2", "3x4_D2_T5_dc3", "4x4_D1odd_T8_dc3"])
 def test_host_tables_reproduce_the_reference_through_a_dense_sampler(name):
     z, meta, sites, mk = _golden(name)
     lat = load_lattice(os.path.join(GOLDEN, f"tv_{name}_lattice.pkl")) if name.startswith("3x3") else None
