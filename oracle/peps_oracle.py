@@ -601,3 +601,49 @@ class ObserverAccumulator:
         energy = self.er / self.total_weight
         return [[2 * (self.EDelta[l1][l2] / self.total_weight - energy * self.Delta[l1][l2] / self.total_weight)
                  for l2 in range(self.peps.L2)] for l1 in range(self.peps.L1)]
+
+
+# ----------------------------------------------------------------------------------------------
+# direct sampling, exact (small lattices)
+# ----------------------------------------------------------------------------------------------
+class DirectSamplerExact:
+    """``DirectSampling.__call__`` (tetragono/tetragono/sampling_lattice/sampling.py:276-371) when its
+    single- and double-layer cuts make every contraction exact: site by site in row-major order, one
+    ``uniform_real(0, 1)`` draw per site chooses the physical index from the conditional marginal
+    rho(x) ~ (sum over the unsampled sites of |psi|^2)^alpha, normalised, by the cumulative rule of
+    ``_choice`` (:362-371); the returned possibility is the product of the chosen rho.  The marginals
+    come from enumerating every configuration (P^(L1 L2) amplitudes; small lattices only)."""
+
+    def __init__(self, peps, engine, alpha=1.0):
+        import itertools
+        self.peps, self.engine, self.alpha = peps, engine, alpha
+        P = peps.A[0][0].shape[0]
+        n = peps.L1 * peps.L2
+        self.P, self.n = P, n
+        w = np.zeros((P,) * n)
+        for idx in itertools.product(range(P), repeat=n):
+            conf = np.array(idx).reshape(peps.L1, peps.L2)
+            w[idx] = Environment(peps, conf).amplitude()**2
+        self.w = w
+
+    def __call__(self):
+        chosen = []
+        possibility = 1.0
+        for k in range(self.n):
+            marg = self.w[tuple(chosen)]
+            rho = marg.reshape(self.P, -1).sum(axis=1)
+            rho = np.maximum(rho, 0.0)
+            if rho.sum() == 0:
+                raise NotImplementedError("zero marginal: the reference redraws the whole sample")
+            rho = rho**self.alpha
+            rho = rho / rho.sum()
+            p = uniform_real01(self.engine)
+            choice = len(rho) - 1
+            for i, r in enumerate(rho):
+                p -= r
+                if p < 0:
+                    choice = i
+                    break
+            possibility *= rho[choice]
+            chosen.append(choice)
+        return possibility, np.array(chosen).reshape(self.peps.L1, self.peps.L2)

@@ -295,6 +295,28 @@ def run_checkpoint_case(name, kind, L1, L2, D, tensor_seed):
     print(f"{name}: lattice file saved {os.path.getsize(path)} bytes")
 
 
+def run_direct_case(name, kind, L1, L2, D, tensor_seed, cut, double_cut, runs):
+    """The reference's DirectSampling (tetragono/tetragono/sampling_lattice/sampling.py:252-371) on the
+    lattice of case ``name`` with cuts large enough to be exact; ``runs`` = [(seed, alpha, n_samples)].
+    Saves per run the sampled configurations and possibilities to <name>_direct.npz."""
+    lattice = build_lattice(kind, L1, L2, D, tensor_seed)
+    out = {"runs": np.array(runs, dtype=np.float64), "cuts": np.array([cut, double_cut])}
+    for k, (seed, alpha, n) in enumerate(runs):
+        lattice.attribute["alpha"] = alpha
+        TAT.random.seed(int(seed))
+        sampling = tet.DirectSampling(lattice, cut, None, double_cut)
+        confs, poss = [], []
+        for _ in range(int(n)):
+            p, conf = sampling()
+            confs.append(conf.export_configuration()[:, :, 0].copy())
+            poss.append(p)
+        out[f"confs{k}"] = np.array(confs, dtype=np.int64)
+        out[f"possibility{k}"] = np.array(poss)
+    path = os.path.join(HERE, f"{name}_direct.npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: direct sampling, {len(runs)} runs, saved {os.path.getsize(path)} bytes")
+
+
 def _same_shapes(holes, L1, L2):
     return False
 
@@ -303,6 +325,10 @@ def _pack_holes(holes, L1, L2):
     return [[dense_site(holes[l1][l2]) for l2 in range(L2)] for l1 in range(L1)]
 
 
+if __name__ == "__main__" and "--direct-only" in sys.argv:
+    run_direct_case("heis_no_3x3_D3_dc4", "no", 3, 3, 3, 1234, 64, 256, [(5, 1.0, 12), (6, 0.5, 12)])
+if __name__ == "__main__" and "--direct-only" in sys.argv:
+    sys.exit(0)
 if __name__ == "__main__" and "--natural-only" not in sys.argv and "--checkpoint-only" not in sys.argv:
     run_case("heis_no_3x3_D3_dc4", "no", 3, 3, 3, 4, 1234, [11, 12], 3, 5)
     run_case("heis_no_4x4_D4_dc16", "no", 4, 4, 4, 16, 2024, [21, 22], 4, 6)

@@ -101,3 +101,19 @@ def test_oracle_natural_gradient_matches_reference(name):
             for l2 in range(g.L2):
                 ref = nat[f"natgrad{k}_{l1}_{l2}"]
                 assert np.abs(grad[l1][l2] - ref).max() <= 1e-8 * scale, (k, l1, l2)
+
+
+def test_direct_sampling_matches_reference():
+    """DirectSampling with exact cuts: the reference's sampled configurations (bit-exact) and
+    possibilities, for alpha 1 and 0.5, from the enumeration oracle replaying the same draws."""
+    from oracle.peps_oracle import DensePEPS, DirectSamplerExact
+    from oracle.rng import MT19937_64
+    g = Golden("heis_no_3x3_D3_dc4")
+    z = np.load(os.path.join(GOLDEN, "heis_no_3x3_D3_dc4_direct.npz"))
+    peps = DensePEPS(g.dense_sites(), g.terms(), int(z["cuts"][0]))
+    for k, (seed, alpha, n) in enumerate(z["runs"]):
+        sampler = DirectSamplerExact(peps, MT19937_64(int(seed)), alpha)
+        for i in range(int(n)):
+            p, conf = sampler()
+            np.testing.assert_array_equal(conf, z[f"confs{k}"][i])
+            assert p == pytest.approx(z[f"possibility{k}"][i], rel=1e-12)
