@@ -317,6 +317,56 @@ def run_direct_case(name, kind, L1, L2, D, tensor_seed, cut, double_cut, runs):
     print(f"{name}: direct sampling, {len(runs)} runs, saved {os.path.getsize(path)} bytes")
 
 
+def run_observe_case(name, kind, L1, L2, D, cut, tensor_seed, chain_seeds, n_therm, n_samples):
+    """The chains of case ``name`` observed with an ``observer_set`` of long-range diagonal operators
+    (Sz on single sites, SzSz on distant pairs; tetragono/tetragono/common_tensor/No.py) besides the
+    energy; saves the reference's ``result`` / ``whole_result`` (observer.py:473-503) and the operators'
+    element tables to <name>_observe.npz."""
+    lattice = build_lattice(kind, L1, L2, D, tensor_seed)
+    No = tet.common_tensor.No
+    Sz, SzSz = No.Sz.to(float), No.SzSz.to(float)
+    observer_set = {
+        "SzSz": {((0, 0, 0), (2, 2, 0)): SzSz, ((0, 1, 0), (2, 1, 0)): SzSz, ((1, 0, 0), (1, 2, 0)): SzSz},
+        "Sz": {((1, 1, 0),): Sz, ((0, 2, 0),): Sz},
+    }
+    neel = np.zeros((L1, L2, 1), dtype=np.int64)
+    for l1 in range(L1):
+        for l2 in range(L2):
+            neel[l1, l2, 0] = (l1 + l2) % 2
+    observer = tet.Observer(lattice, observer_set={k: dict(v) for k, v in observer_set.items()}, enable_energy=True)
+    with observer:
+        for seed in chain_seeds:
+            TAT.random.seed(seed)
+            sampling = tet.SweepSampling(lattice, cut, None, None)
+            sampling.configuration.import_configuration(neel)
+            for step in range(n_therm + n_samples):
+                possibility, configuration = sampling()
+                if step >= n_therm:
+                    observer(possibility, configuration)
+    phys = lattice.physics_edges[0, 0, 0]
+    out, meta = {}, {"names": [], "positions": []}
+    result, whole = observer.result, observer.whole_result
+    k = 0
+    for nm, terms in observer_set.items():
+        for positions, H in terms.items():
+            rows = []
+            for s_in, outs in tensor_element(H).items():
+                for s_out, value in outs.items():
+                    rows.append([point_index(phys, p) for p in s_in] + [point_index(phys, p) for p in s_out] +
+                                [float(value.storage[0])])
+            out[f"table_{k}"] = np.array(rows)
+            out[f"result_{k}"] = np.array(result[nm][positions])
+            meta["names"].append(nm)
+            meta["positions"].append([list(p) for p in positions])
+            k += 1
+        out[f"whole_{nm}"] = np.array(whole[nm])
+    out["energy"] = np.array(observer.energy)
+    out["meta"] = np.array(json.dumps(meta))
+    path = os.path.join(HERE, f"{name}_observe.npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: observer set of {k} terms, saved {os.path.getsize(path)} bytes")
+
+
 def _same_shapes(holes, L1, L2):
     return False
 
@@ -327,6 +377,7 @@ def _pack_holes(holes, L1, L2):
 
 if __name__ == "__main__" and "--direct-only" in sys.argv:
     run_direct_case("heis_no_3x3_D3_dc4", "no", 3, 3, 3, 1234, 64, 256, [(5, 1.0, 12), (6, 0.5, 12)])
+    run_observe_case("heis_no_3x3_D3_dc4", "no", 3, 3, 3, 4, 1234, [11, 12], 3, 5)
 if __name__ == "__main__" and "--direct-only" in sys.argv:
     sys.exit(0)
 if __name__ == "__main__" and "--natural-only" not in sys.argv and "--checkpoint-only" not in sys.argv:

@@ -156,11 +156,14 @@ class SweepSampling:
             if self._engine._uploaded_version != self.owner.version:
                 self._engine.upload()
             self._engine.sweep(1, observe=observing)
-            if observing and observer._enable_natural:
-                eloc, _, reweight = self._engine.read_samples(1)
-                observer._samples_e.extend(eloc[0].tolist())
-                observer._samples_w.extend(reweight[0].tolist())
             conf, logp = self._engine.read_chains()
+            if observing and (observer._enable_natural or observer._observer_set):
+                eloc, _, reweight = self._engine.read_samples(1)
+                if observer._enable_natural:
+                    observer._samples_e.extend(eloc[0].tolist())
+                    observer._samples_w.extend(reweight[0].tolist())
+                if observer._observer_set:
+                    observer._observe_diagonal(conf, reweight[0])
             self._buffer = [(float(np.exp(lp)), Configuration(self.owner, c), observing) for c, lp in zip(conf, logp)]
             self._buffer.reverse()
         possibility, configuration, observed = self._buffer.pop()
@@ -175,10 +178,32 @@ class Observer:
     def __init__(self, owner, *, observer_set=None, enable_energy=False, enable_gradient=False,
                  enable_natural_gradient=False, cache_natural_delta=None, cache_configuration=False,
                  restrict_subspace=None, classical_energy=None):
-        if observer_set or cache_natural_delta or cache_configuration or restrict_subspace is not None or \
-                classical_energy is not None:
-            raise NotImplementedError("only energy, gradient and natural-gradient observation are supported")
+        if cache_natural_delta or cache_configuration or restrict_subspace is not None or classical_energy is not None:
+            raise NotImplementedError("only energy, gradient, natural-gradient and diagonal observer-set observation "
+                                      "are supported")
         self.owner = owner
+        # observer_set: {name: {positions: element table}}, tables as the lattice's Hamiltonian tables
+        # ({input tuple: [(output tuple, value)]}); diagonal operators only (their value needs the sampled
+        # configuration alone, as Sz or n at any distance)
+        self._observer_set = {}
+        for name, terms in (observer_set or {}).items():
+            if name == "energy":
+                raise ValueError("the name 'energy' is reserved for the Hamiltonian")
+            entries = []
+            for positions, table in terms.items():
+                positions = tuple(tuple(p) for p in positions)
+                if any(p[2] != 0 for p in positions):
+                    raise NotImplementedError("only orbit 0 is supported")
+                diag = {}
+                for s_in, outs in table.items():
+                    for s_out, value in outs:
+                        if tuple(s_out) != tuple(s_in):
+                            raise NotImplementedError(f"observer '{name}' at {positions}: off-diagonal elements need "
+                                                      "replacement amplitudes, which are not supported")
+                        diag[tuple(s_in)] = diag.get(tuple(s_in), 0.0) + float(value)
+                entries.append((positions, diag))
+            self._observer_set[name] = entries
+        self._set_acc = None
         self._enable_natural = bool(enable_natural_gradient)
         self._enable_energy = enable_energy or enable_gradient or self._enable_natural
         self._enable_gradient = enable_gradient or self._enable_natural
@@ -198,8 +223,26 @@ class Observer:
         self._scalars = None
         self._samples_e = []
         self._samples_w = []
+        self._set_acc = {name: (np.zeros((len(entries), 3)), np.zeros(3)) for name, entries in self._observer_set.items()}
         self.owner._active_observer = self
         return self
+
+    def _observe_diagonal(self, confs, reweights):
+        """Observer.__call__ (observer.py:344-402) for the diagonal observer set: per sample with nonzero
+        weight w and per term the value x = <s|O|s>, summing x w, x w^2 and x^2 w^2, and the same for the
+        sum over a name's terms."""
+        for conf, w in zip(confs, reweights):
+            if w == 0.0:
+                continue
+            conf = np.asarray(conf).reshape(self.owner.L1, self.owner.L2)
+            for name, entries in self._observer_set.items():
+                acc, whole = self._set_acc[name]
+                total = 0.0
+                for k, (positions, diag) in enumerate(entries):
+                    x = diag.get(tuple(int(conf[p[0], p[1]]) for p in positions), 0.0)
+                    acc[k] += (x * w, x * w * w, x * x * w * w)
+                    total += x
+                whole += (total * w, total * w * w, total * total * w * w)
 
     def _bind(self, engine):
         if self._engine is not None:
@@ -215,7 +258,45 @@ class Observer:
         if self._engine is not None:
             self._scalars, self._delta, self._edelta = self._reduced(
                 *self._engine.read_observer(with_gradient=self._enable_gradient))
+        if self._set_acc:
+            names = list(self._set_acc)
+            flat = np.concatenate([np.concatenate([a.ravel(), w]) for a, w in (self._set_acc[n] for n in names)])
+            (flat,) = allreduce_sum([flat])
+            pos = 0
+            for n in names:
+                a, w = self._set_acc[n]
+                a[...] = flat[pos:pos + a.size].reshape(a.shape)
+                pos += a.size
+                w[...] = flat[pos:pos + 3]
+                pos += 3
         return False
+
+    def _expect(self, sums):
+        """``_expect_and_deviation`` (observer.py:433-469) with the totals of the weights."""
+        s = self._read()
+        R, RR = s[1], s[2]
+        ER, ERR, EERR = sums
+        if ER == 0.0 or R == 0.0:
+            return 0.0, 0.0
+        expect = ER / R
+        variance = (EERR - 2 * ERR * expect + RR * expect**2) / R**2
+        return expect, (variance**0.5 if variance >= 0.0 else 0.0)
+
+    @property
+    def result(self):
+        """``Observer.result``: {name: {positions: (expect, deviation)}} of the observer set."""
+        return {name: {positions: self._expect(self._set_acc[name][0][k])
+                       for k, (positions, _) in enumerate(entries)}
+                for name, entries in self._observer_set.items()}
+
+    @property
+    def whole_result(self):
+        """``Observer.whole_result``: {name: (expect, deviation)} of each name's summed terms, and the
+        energy."""
+        out = {name: self._expect(self._set_acc[name][1]) for name in self._observer_set}
+        if self._enable_energy:
+            out["energy"] = self.total_energy
+        return out
 
     def _reduced(self, scalars, delta, edelta):
         """Sum over the ranks of a process group (one collective), as ``Observer.__exit__`` does."""
