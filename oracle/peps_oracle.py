@@ -28,7 +28,9 @@ What is restated, with the reference lines it follows:
 * ``SweepSampling._single_term`` / ``__call__`` / ``_get_proper_position_order``
   (tetragono/tetragono/sampling_lattice/sampling.py:117-190);
 * ``Observer.__call__`` and the estimators (tetragono/tetragono/sampling_lattice/observer.py:313-415,
-  433-469, 528-555).
+  433-469, 528-555);
+* ``DirectSampling.__call__`` with exact cuts (tetragono/tetragono/sampling_lattice/sampling.py:276-371),
+  its marginals by enumeration (``DirectSamplerExact``, small lattices).
 
 With charges (Bose U(1)) every QR and SVD of the compression is done per charge sector, with the
 truncation keeping the largest singular values over all sectors, as TAT's block-sparse qr / svd
