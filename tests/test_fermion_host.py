@@ -261,3 +261,33 @@ def test_sampler_inputs_of_a_fermionic_lattice():
             np.testing.assert_array_equal(folded[a][b], fl.fold_gradient(a, b, raw[a][b]))
     n, sites, offs, cnts, outs, vals = lat.term_arrays()
     assert n == len(fl.terms) == 3 * 3 + 2 * 4
+
+
+def test_fermionic_lattice_file_write_back():
+    """New dense tensors written into a reference t-V lattice file come back from our reader, and the
+    reference's own loader reads the file (when the reference is present)."""
+    path = os.path.join(GOLDEN, "tv_3x4_D2_T5_dc3_lattice.pkl")
+    ref = load_lattice(path)
+    lat = F.from_reference_lattice(ref)
+    new = [[-0.5 * lat.tensors[a][b] for b in range(lat.L2)] for a in range(lat.L1)]
+    F.set_reference_tensors(ref, new)
+    buf = io.BytesIO()
+    save_lattice(ref, buf)
+    buf.seek(0)
+    back = F.from_reference_lattice(load_lattice(buf))
+    for a in range(lat.L1):
+        for b in range(lat.L2):
+            np.testing.assert_array_equal(back.tensors[a][b], new[a][b])
+            assert back.edges[a][b] == lat.edges[a][b]
+    bad = [[t.copy() for t in row] for row in new]
+    zero = np.argwhere(bad[1][1] == 0)[0]
+    bad[1][1][tuple(zero)] = 1.0
+    with pytest.raises(ValueError):
+        F.set_reference_tensors(load_lattice(path), bad)
+    from test_checkpoint import _reference_modules
+    _reference_modules()   # skips when the reference is not available
+    import pickle
+    theirs = pickle.loads(buf.getvalue())
+    for a in range(lat.L1):
+        for b in range(lat.L2):
+            np.testing.assert_array_equal(np.array(theirs[a, b].storage), ref.state["_lattice"][a][b].storage)

@@ -163,6 +163,22 @@ class FermionLattice:
         return dense_to_blocks(arr, edges)
 
 
+def set_reference_tensors(ref, tensors):
+    """Writes dense site tensors ``tensors[l1][l2]`` (p, u, d, l, r, the layout of FermionLattice) into
+    the block storage of a fermionic lattice file read by ``tnsp_gb300.checkpoint.load_lattice`` (edges
+    and arrows unchanged), so that ``save_lattice`` writes a file the reference loads; entries outside
+    the charge blocks must be zero."""
+    lat = from_reference_lattice(ref)
+    st = ref.state
+    for l1 in range(lat.L1):
+        for l2 in range(lat.L2):
+            storage = lat.to_blocks(l1, l2, tensors[l1][l2])
+            back = site_from_blocks(storage, lat.names[l1][l2], [segs for segs, _ in lat.edges[l1][l2]])
+            if not np.array_equal(back, np.asarray(tensors[l1][l2])):
+                raise ValueError(f"site ({l1}, {l2}) has nonzero entries outside its symmetry blocks")
+            st["_lattice"][l1][l2].storage = storage
+
+
 def configuration_sign(conf, p_T, family):
     """prod over cuts k of (-1)^((N_<k + p_T)(N_<=k + p_T)), N counting the particles of the rows
     (row-major) or columns (column-major) before / up to k."""
@@ -327,4 +343,4 @@ def _block_storage_size(edges):
 
 
 __all__ = ["FermionLattice", "configuration_sign", "hop_sign", "order_inversions", "vertical_pair_sign",
-           "tv_element_table", "from_reference_lattice", "random_tv"]
+           "tv_element_table", "from_reference_lattice", "set_reference_tensors", "random_tv"]
