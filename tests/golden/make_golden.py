@@ -367,6 +367,28 @@ def run_observe_case(name, kind, L1, L2, D, cut, tensor_seed, chain_seeds, n_the
     print(f"{name}: observer set of {k} terms, saved {os.path.getsize(path)} bytes")
 
 
+def run_ergodic_case(name, kind, L1, L2, D, cut, tensor_seed):
+    """The reference's ErgodicSampling (tetragono/tetragono/sampling_lattice/sampling.py:196-249) over every
+    configuration of the lattice of case ``name`` with an energy Observer: the exact energy of the
+    truncated-contraction PEPS (no sampling noise).  Saves it to <name>_ergodic.npz."""
+    lattice = build_lattice(kind, L1, L2, D, tensor_seed)
+    sampling = tet.ErgodicSampling(lattice, cut, None)
+    observer = tet.Observer(lattice, enable_energy=True, enable_gradient=True)
+    with observer:
+        for _ in range(sampling.total_step):
+            possibility, configuration = sampling()
+            observer(possibility, configuration)
+    out = {"energy": np.array(observer.energy), "total_energy": np.array(observer.total_energy),
+           "total_steps": np.array(sampling.total_step), "cut": np.array(cut)}
+    grad = observer.gradient
+    for l1 in range(L1):
+        for l2 in range(L2):
+            out[f"grad_{l1}_{l2}"] = dense_site(grad[l1][l2])
+    path = os.path.join(HERE, f"{name}_ergodic.npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: ergodic E/site = {observer.energy[0]:.12f}, saved {os.path.getsize(path)} bytes")
+
+
 def _same_shapes(holes, L1, L2):
     return False
 
@@ -378,6 +400,7 @@ def _pack_holes(holes, L1, L2):
 if __name__ == "__main__" and "--direct-only" in sys.argv:
     run_direct_case("heis_no_3x3_D3_dc4", "no", 3, 3, 3, 1234, 64, 256, [(5, 1.0, 12), (6, 0.5, 12)])
     run_observe_case("heis_no_3x3_D3_dc4", "no", 3, 3, 3, 4, 1234, [11, 12], 3, 5)
+    run_ergodic_case("heis_no_3x3_D3_dc4", "no", 3, 3, 3, 4, 1234)
 if __name__ == "__main__" and "--direct-only" in sys.argv:
     sys.exit(0)
 if __name__ == "__main__" and "--natural-only" not in sys.argv and "--checkpoint-only" not in sys.argv:

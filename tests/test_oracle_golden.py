@@ -117,3 +117,22 @@ def test_direct_sampling_matches_reference():
             p, conf = sampler()
             np.testing.assert_array_equal(conf, z[f"confs{k}"][i])
             assert p == pytest.approx(z[f"possibility{k}"][i], rel=1e-12)
+
+
+def test_ergodic_energy_and_gradient_match_reference():
+    """ErgodicSampling (every configuration, possibility 1, sampling.py:196-249) with the truncating cut
+    of the golden case: the oracle's exact enumeration of E/site, its error bar and the gradient against
+    the reference's, free of sampling noise."""
+    import itertools
+    g = Golden("heis_no_3x3_D3_dc4")
+    z = np.load(os.path.join(GOLDEN, "heis_no_3x3_D3_dc4_ergodic.npz"))
+    peps = DensePEPS(g.dense_sites(), g.terms(), int(z["cut"]))
+    acc = ObserverAccumulator(peps)
+    for idx in itertools.product(range(2), repeat=9):
+        acc.add(1.0, np.array(idx).reshape(3, 3))  # the order of the sum does not matter
+    assert acc.count == int(z["total_steps"])
+    np.testing.assert_allclose(acc.energy(), z["energy"], rtol=1e-11)
+    grad = acc.gradient()
+    for l1 in range(3):
+        for l2 in range(3):
+            np.testing.assert_allclose(grad[l1][l2], z[f"grad_{l1}_{l2}"], rtol=1e-9, atol=1e-12)
