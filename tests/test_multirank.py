@@ -203,3 +203,72 @@ def test_two_rank_natural_gradient_equals_one_process():
         want = _natgrad_single(rows, w, e, step, error)
         for rank, results in out:
             np.testing.assert_allclose(results[k], want, rtol=1e-10, atol=1e-12)
+
+
+def _observer_set_worker(rank, world, port, q):
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import numpy as np
+    from tnsp_gb300.sampling import Observer
+    from test_multirank import _FakeEngine, _FakeOwner3, _observer_set_data
+    confs, w, e, sets = _observer_set_data()
+    mine = slice(rank, None, world)
+    obs = Observer(_FakeOwner3(), observer_set=sets, enable_energy=True)
+    obs.__enter__()
+    obs._bind(_FakeEngine(np.zeros((len(w[mine]), 1)), w[mine], e[mine]))
+    obs._observe_diagonal(confs[mine], w[mine])
+    obs.__exit__(None, None, None)
+    res = obs.result
+    q.put((rank, {n: {str(k): v for k, v in d.items()} for n, d in res.items()}, obs.whole_result))
+    dist.destroy_process_group()
+
+
+class _FakeOwner3:
+    L1 = L2 = 3
+    site_number = 9
+    _active_observer = None
+
+
+def _observer_set_data():
+    import numpy as np
+    rng = np.random.default_rng(31)
+    confs = (rng.random((12, 3, 3)) < 0.5).astype(np.int64)
+    w = rng.random(12) + 0.2
+    e = rng.normal(size=12)
+    sz = {(0,): [((0,), 0.5)], (1,): [((1,), -0.5)]}
+    szsz = {(a, b): [((a, b), 0.25 * (1 - 2 * a) * (1 - 2 * b))] for a in (0, 1) for b in (0, 1)}
+    sets = {"Sz": {((1, 1, 0),): sz, ((2, 0, 0),): sz}, "SzSz": {((0, 0, 0), (2, 2, 0)): szsz}}
+    return confs, w, e, sets
+
+
+def test_two_rank_observer_set_equals_one_process():
+    """Diagonal observer-set accumulators split over two gloo ranks are summed like the reference's
+    MPI reduction: results equal the one-process ones."""
+    import numpy as np
+    from tnsp_gb300.sampling import Observer
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_observer_set_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    confs, w, e, sets = _observer_set_data()
+    one = Observer(_FakeOwner3(), observer_set=sets, enable_energy=True)
+    one.__enter__()
+    one._bind(_FakeEngine(np.zeros((len(w), 1)), w, e))
+    one._observe_diagonal(confs, w)
+    one.__exit__(None, None, None)
+    want = {n: {str(k): v for k, v in d.items()} for n, d in one.result.items()}
+    for rank, res, whole in out:
+        for n in want:
+            for k in want[n]:
+                np.testing.assert_allclose(res[n][k], want[n][k], rtol=1e-12)
+            np.testing.assert_allclose(whole[n], one.whole_result[n], rtol=1e-12)
+        np.testing.assert_allclose(whole["energy"], one.whole_result["energy"], rtol=1e-12)
