@@ -399,6 +399,8 @@ def _pack_holes(holes, L1, L2):
 
 if __name__ == "__main__" and "--direct-only" in sys.argv:
     run_direct_case("heis_no_3x3_D3_dc4", "no", 3, 3, 3, 1234, 64, 256, [(5, 1.0, 12), (6, 0.5, 12)])
+    run_direct_case("heis_no_3x3_D3_dc4_trunc", "no", 3, 3, 3, 1234, 4, 6, [(5, 1.0, 12), (6, 0.5, 12)])
+    run_direct_case("heis_no_3x3_D3_dc4_trunc2", "no", 3, 3, 3, 1234, 2, 4, [(7, 1.0, 12), (8, 0.5, 12)])
     run_observe_case("heis_no_3x3_D3_dc4", "no", 3, 3, 3, 4, 1234, [11, 12], 3, 5)
     run_ergodic_case("heis_no_3x3_D3_dc4", "no", 3, 3, 3, 4, 1234)
 if __name__ == "__main__" and "--direct-only" in sys.argv:

@@ -136,3 +136,21 @@ def test_ergodic_energy_and_gradient_match_reference():
     for l1 in range(3):
         for l2 in range(3):
             np.testing.assert_allclose(grad[l1][l2], z[f"grad_{l1}_{l2}"], rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", ["heis_no_3x3_D3_dc4_trunc", "heis_no_3x3_D3_dc4_trunc2"])
+def test_direct_sampling_with_truncation_matches_reference(name):
+    """DirectSampling with truncating single- and double-layer cuts, (4, 6) and (2, 4)
+    (oracle/direct_oracle.py): the reference's samples, configurations bit-exact and possibilities to
+    1e-12, alpha 1 and 0.5."""
+    from oracle.direct_oracle import DirectSampler
+    g = Golden("heis_no_3x3_D3_dc4")
+    z = np.load(os.path.join(GOLDEN, f"{name}_direct.npz"))
+    cuts = tuple(int(x) for x in z["cuts"])
+    peps = DensePEPS(g.dense_sites(), g.terms(), cuts[0])
+    for k, (seed, alpha, n) in enumerate(z["runs"]):
+        sampler = DirectSampler(peps, MT19937_64(int(seed)), cuts[1], alpha)
+        for i in range(int(n)):
+            p, conf = sampler()
+            np.testing.assert_array_equal(conf, z[f"confs{k}"][i])
+            assert p == pytest.approx(z[f"possibility{k}"][i], rel=1e-12)
