@@ -598,6 +598,31 @@ class ObserverAccumulator:
             out.append(row)
         return out, t
 
+    def natural_gradient_pinv(self, r_pinv, a_pinv):
+        """``natural_gradient_by_direct_pseudo_inverse`` (observer.py:697-907) by its single-process
+        equation (observer.py:902-907): T = D D^T with unweighted rows D_s = delta_s - <delta>,
+        L^+ = 1 / (L (1 + ((r max L + a) / L)^6)) on L > 0, NG = D^T U L^+ U^T (E - <E>); returns 2 NG
+        per site."""
+        if self.samples is None:
+            raise RuntimeError("natural gradient not enabled")
+        W = self.total_weight
+        delta = np.concatenate([d.ravel() for row in self.Delta for d in row]) / W
+        D = np.array([h - delta for _, _, h in self.samples])
+        E = np.array([e for _, e, _ in self.samples]) - self.er / W
+        L, U = np.linalg.eigh(D @ D.T)
+        num = r_pinv * L.max() + a_pinv
+        Linv = np.array([0.0 if l <= 0 else 1.0 / (l * (1 + (num / l)**6)) for l in L])
+        x = 2 * (D.T @ (U @ (Linv * (U.T @ E))))
+        out, o = [], 0
+        for l1 in range(self.peps.L1):
+            row = []
+            for l2 in range(self.peps.L2):
+                n = self.peps.A[l1][l2].size
+                row.append(x[o:o + n].reshape(self.peps.A[l1][l2].shape))
+                o += n
+            out.append(row)
+        return out
+
     def gradient(self):
         """``Observer.gradient`` (observer.py:542-555) for real tensors."""
         energy = self.er / self.total_weight

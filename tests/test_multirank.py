@@ -272,3 +272,33 @@ def test_two_rank_observer_set_equals_one_process():
                 np.testing.assert_allclose(res[n][k], want[n][k], rtol=1e-12)
             np.testing.assert_allclose(whole[n], one.whole_result[n], rtol=1e-12)
         np.testing.assert_allclose(whole["energy"], one.whole_result["energy"], rtol=1e-12)
+
+
+def test_pseudo_inverse_natural_gradient_in_one_process():
+    """The drop-in pseudo-inverse natural gradient (single-process form of observer.py:697-907) on rows
+    held by a stand-in engine: against the same equation evaluated directly, and, with a tiny
+    regulariser, x / 2 solves the least-squares equations D^T D (x / 2) = D^T (E - <E>).  (T = D D^T
+    always has the weight vector as a null vector, so some regularisation is required.)"""
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    from tnsp_gb300.sampling import Observer
+    rows, w, e = _natgrad_data()
+    for r_pinv, a_pinv in [(1e-6, 1e-9), (1e-3, 1e-12), (1e-9, 0.0)]:
+        obs = Observer(_FakeOwner(), enable_natural_gradient=True)
+        obs.__enter__()
+        obs._bind(_FakeEngine(rows, w, e))
+        obs._samples_w = w.tolist()
+        obs._samples_e = e.tolist()
+        obs.__exit__(None, None, None)
+        x = obs.natural_gradient_by_direct_pseudo_inverse(r_pinv, a_pinv)
+        W = w.sum()
+        delta = (w[:, None] * rows).sum(axis=0) / W
+        D = rows - delta
+        E = e - (w * e).sum() / W
+        L, U = np.linalg.eigh(D @ D.T)
+        num = r_pinv * L.max() + a_pinv
+        Linv = np.array([0.0 if l <= 0 else 1.0 / (l * (1 + (num / l)**6)) for l in L])
+        want = 2 * D.T @ (U @ (Linv * (U.T @ E)))
+        np.testing.assert_allclose(x, want, rtol=1e-8, atol=1e-12)
+        if r_pinv == 1e-9:
+            np.testing.assert_allclose(D.T @ (D @ (x / 2)), D.T @ E, rtol=1e-6, atol=1e-9)

@@ -154,3 +154,25 @@ def test_direct_sampling_with_truncation_matches_reference(name):
             p, conf = sampler()
             np.testing.assert_array_equal(conf, z[f"confs{k}"][i])
             assert p == pytest.approx(z[f"possibility{k}"][i], rel=1e-12)
+
+
+def test_pseudo_inverse_natural_gradient_meets_the_reference_conjugate_gradient():
+    """The pseudo-inverse natural gradient (observer.py:697-907, by its single-process equation; the
+    reference's ScaLAPACK path cannot run here) and the reference's own conjugate-gradient natural
+    gradient solve the same least-squares problem (reweights 1, fewer samples than parameters: both give
+    the least-norm solution); they agree to the conjugate gradient's stopping tolerance of 1e-3."""
+    g = Golden("heis_no_3x3_D3_dc4")
+    nat = np.load(os.path.join(GOLDEN, "heis_no_3x3_D3_dc4_natgrad.npz"))
+    peps = DensePEPS(g.dense_sites(), g.terms(), g.cut)
+    acc = ObserverAccumulator(peps, natural=True)
+    for seed in g.meta["chain_seeds"]:
+        chain = SweepChain(peps, g.neel(), seed)
+        for k in range(g.meta["n_therm"] + g.meta["n_samples"]):
+            poss, conf = chain.sweep()
+            if k >= g.meta["n_therm"]:
+                acc.add(poss, conf, chain.env)
+    k = [i for i, (s, e) in enumerate(nat["runs"]) if e > 0][0]
+    pinv = acc.natural_gradient_pinv(1e-8, 0.0)
+    scale = max(np.abs(nat[f"natgrad{k}_{a}_{b}"]).max() for a in range(g.L1) for b in range(g.L2))
+    err = max(np.abs(pinv[a][b] - nat[f"natgrad{k}_{a}_{b}"]).max() for a in range(g.L1) for b in range(g.L2))
+    assert err <= 2e-3 * scale

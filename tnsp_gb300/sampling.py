@@ -391,6 +391,42 @@ class Observer:
         self.natural_gradient_steps = t
         return self.owner.unflatten(self._fold(2 * x))
 
+    def natural_gradient_by_direct_pseudo_inverse(self, r_pinv, a_pinv, libraries=None):
+        """``Observer.natural_gradient_by_direct_pseudo_inverse`` (observer.py:697-907) in one process, the
+        equation of its single-process form (observer.py:902-907): with D_s = delta_s - <delta> over the
+        kept samples (unweighted rows) and E_s = E_loc,s - <E>, T = D D^T = U diag(L) U^T,
+        L^+ = 1 / (L (1 + ((r_pinv max L + a_pinv) / L)^6)) for L > 0 (0 otherwise), and the result
+        2 D^T U L^+ U^T E per site.  T is built from products with the rows kept on the device
+        (``tnsp_holes_gemv``); the reference distributes the samples with ScaLAPACK, so several ranks
+        raise NotImplementedError here (use the conjugate gradient).  ``libraries`` is accepted and not
+        used."""
+        if not self._enable_natural:
+            raise RuntimeError("natural gradient not enabled")
+        if _process_group()[1] > 1:
+            raise NotImplementedError("the pseudo-inverse natural gradient runs in one process; use the conjugate "
+                                      "gradient with several ranks")
+        scal = self._read()
+        W = scal[1]
+        delta = np.asarray(self._delta) / W
+        En = np.asarray(self._samples_e) - scal[4] / W
+        eng = self._engine
+        n = len(En)
+        T = np.empty((n, n))
+        unit = np.zeros(n)
+        for j in range(n):
+            unit[j] = 1.0
+            col = eng.holes_gemv(unit, transpose=True) - delta      # D^T e_j
+            T[:, j] = eng.holes_gemv(col) - np.dot(delta, col)       # D D^T e_j
+            unit[j] = 0.0
+        T = 0.5 * (T + T.T)
+        L, U = np.linalg.eigh(T)
+        num = r_pinv * L[-1] + a_pinv
+        safe = np.where(L > 0, L, 1.0)
+        Linv = np.where(L > 0, 1.0 / (safe * (1.0 + (num / safe)**6)), 0.0)
+        y = U @ (Linv * (U.T @ En))
+        x = 2 * (eng.holes_gemv(y, transpose=True) - delta * y.sum())
+        return self.owner.unflatten(self._fold(x))
+
     @property
     def instability(self):
         s = self._read()
