@@ -291,3 +291,13 @@ def test_fermionic_lattice_file_write_back():
     for a in range(lat.L1):
         for b in range(lat.L2):
             np.testing.assert_array_equal(np.array(theirs[a, b].storage), ref.state["_lattice"][a][b].storage)
+
+
+def test_tv_builder_sector_dimensions():
+    """An int D and the equal triple (D, D, D) build the same layout (tetraku's [(0, D)] interior bonds)."""
+    a = F.random_tv(3, 3, 2, 4, seed=1)
+    b = F.random_tv(3, 3, (2, 2, 2), 4, seed=1)
+    assert a.edges == b.edges
+    for r1, r2 in zip(a.tensors, b.tensors):
+        for t1, t2 in zip(r1, r2):
+            np.testing.assert_array_equal(t1, t2)

@@ -287,7 +287,7 @@ def random_tv(L1, L2, D, particles, seed, interior=None, t=1.0, V=1.0, scale=Tru
         Q = int(T * (L1 - l1 - 1) / L1)
         bonds_d[l1, 0] = [(Q - 1, dims[0]), (Q, dims[1]), (Q + 1, dims[2])]
         for l2 in range(1, L2):
-            bonds_d[l1, l2] = list(interior) if interior is not None else [(0, dims[1] if len(set(dims)) > 1 else D)]
+            bonds_d[l1, l2] = list(interior) if interior is not None else [(0, dims[1])]
     bonds_r = {}
     tt = T / L1
     for l1 in range(L1):
