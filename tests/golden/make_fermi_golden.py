@@ -151,15 +151,26 @@ def _tensor_record(t):
 
 
 def run_tv_case(name, L1, L2, D, T, cut, tensor_seed, chain_seeds, n_therm, n_samples, save_lattice=False,
-                interior=None):
+                interior=None, dims=None, holes=True):
     """Sweep chains of the reference on a t-V lattice (t = V = 1); records per sample the amplitude
-    tensor hole(()) and E_loc (observer.py:313-415)."""
+    tensor hole(()) and E_loc (observer.py:313-415).  ``dims`` = (d-, d0, d+) replaces tetraku's equal
+    sector dimensions D on the R bonds and the column-0 D bonds (the 8x8 workload's (2, 4, 2));
+    ``holes`` False leaves out the per-sample holes (benchmark-size lattices)."""
     sys.argv = sys.argv[:1] + [a for a in sys.argv[1:] if not a.startswith("--")]
     import make_golden  # noqa: F401  (mpi4py stand-in and the reference's paths)
     import tetragono as tet
     from tetraku.models import tV
 
     state = tV.abstract_lattice(L1, L2, D, T, 1.0, 1.0)
+    if dims is not None:
+        # tetraku's charge flow Q on these bonds, with per-sector dimensions
+        for l1 in range(L1 - 1):
+            Q = int(T * (L1 - l1 - 1) / L1)
+            state.virtual_bond[l1, 0, "D"] = [(Q - 1, dims[0]), (Q, dims[1]), (Q + 1, dims[2])]
+        for l1 in range(L1):
+            for l2 in range(L2 - 1):
+                Q = int(T / L1 * (L2 - l2 - 1) / L2)
+                state.virtual_bond[l1, l2, "R"] = [(Q - 1, dims[0]), (Q, dims[1]), (Q + 1, dims[2])]
     if interior is not None:
         # interior D bonds with odd charges (the 8x8 workload's {-1, 0, +1} layout, scaled down)
         for l1 in range(L1 - 1):
@@ -171,7 +182,8 @@ def run_tv_case(name, L1, L2, D, T, cut, tensor_seed, chain_seeds, n_therm, n_sa
         for l2 in range(L2):
             t = lattice[l1, l2]
             z = sum(1 for n in t.names if str(n) in ("U", "D", "L", "R"))
-            lattice[l1, l2] = t * (1.0 / np.sqrt(2.0 * (3 * D)**z))
+            bond = sum(dims) if dims is not None else 3 * D
+            lattice[l1, l2] = t * (1.0 / np.sqrt(2.0 * bond**z))
     out, meta = {}, {"name": name, "L1": L1, "L2": L2, "D": D, "T": T, "cut": cut, "tensor_seed": tensor_seed,
                      "chain_seeds": chain_seeds, "n_therm": n_therm, "n_samples": n_samples, "sites": {},
                      "terms": []}
@@ -196,6 +208,7 @@ def run_tv_case(name, L1, L2, D, T, cut, tensor_seed, chain_seeds, n_therm, n_sa
             break
     observer = tet.Observer(lattice, enable_energy=True, enable_gradient=True)
     confs, poss, ws_names, ws_value, eloc = [], [], [], [], []
+    want_holes = holes
     holes = {f"{a},{b}": [] for a in range(L1) for b in range(L2)}
     with observer:
         for seed in chain_seeds:
@@ -216,6 +229,8 @@ def run_tv_case(name, L1, L2, D, T, cut, tensor_seed, chain_seeds, n_therm, n_sa
                 ws_names.append([str(n) for n in ws.names])
                 ws_value.append(w)
                 eloc.append((observer._whole_result_reweight["energy"] - before) / reweight)
+                if not want_holes:
+                    continue
                 hs = configuration.holes()
                 for a in range(L1):
                     for b in range(L2):
@@ -235,7 +250,8 @@ def run_tv_case(name, L1, L2, D, T, cut, tensor_seed, chain_seeds, n_therm, n_sa
     meta["gradient"] = {}
     for a in range(L1):
         for b in range(L2):
-            out[f"holes_{a}_{b}"] = np.array(holes[f"{a},{b}"])
+            if want_holes:
+                out[f"holes_{a}_{b}"] = np.array(holes[f"{a},{b}"])
             desc, st = _tensor_record(grad[a][b])
             meta["gradient"][f"{a},{b}"] = desc
             out[f"grad_{a}_{b}"] = st
@@ -294,6 +310,15 @@ def run_tv_natural(name, L1, L2, D, T, cut, tensor_seed, chain_seeds, n_therm, n
     print(f"tv_{name}: natural gradient for {len(runs)} settings, {os.path.getsize(path)} bytes")
 
 
+if __name__ == "__main__" and "--workloads" in sys.argv:
+    # the 8x8 fermionic workload: 32 particles, {Q-1:2, Q:4, Q+1:2} on the R and column-0 D bonds,
+    # {-1:2, 0:4, +1:2} on the interior D bonds, Dcut 64 (seconds per sample here: one chain, few sweeps)
+    sys.path.insert(0, HERE)
+    run_tv_case("8x8_D242_T32_dc24", 8, 8, 2, 32, 24, 919, [93, 94], 1, 2, interior=[(-1, 2), (0, 4), (1, 2)],
+                dims=(2, 4, 2), holes=False)
+    run_tv_case("8x8_D242_T32_dc64", 8, 8, 2, 32, 64, 919, [93], 1, 1, interior=[(-1, 2), (0, 4), (1, 2)],
+                dims=(2, 4, 2), holes=False)
+    sys.exit(0)
 if __name__ == "__main__":
     sys.path.insert(0, HERE)
     both = "--ops" not in sys.argv and "--tv" not in sys.argv
