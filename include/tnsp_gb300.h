@@ -51,6 +51,8 @@ typedef struct tnsp_ctx tnsp_ctx;
  */
 int tnsp_ctx_create(tnsp_ctx** out, int device, void* stream);
 int tnsp_ctx_destroy(tnsp_ctx* ctx);
+/* The message of the context's last failure; with ctx == NULL, the message of the calling thread's
+ * last failed context-free call (tnsp_amplitude_noalloc). */
 const char* tnsp_last_error(tnsp_ctx* ctx);
 
 /*
@@ -109,9 +111,30 @@ int tnsp_model_upload(tnsp_ctx* ctx, int n_terms, const int* sites, const int* o
  * seeds chain b's mt19937_64 exactly as TAT.random.seed does, and `discard` uniform_real draws
  * are skipped first (SeedDiffer draws one, tetragono/tetragono/utility.py:146-150).
  * Replaces: Configuration.import_configuration (lattice.py:181-206) + TAT.random.seed (PyTAT/PyTAT.hpp:89-94).
+ * TNSP_DD is refused (TNSP_E_ARG) for a lattice uploaded without charges whose site tensors are more
+ * than a quarter exact zeros: such block-sparse tensors stored densely make rank-deficient boundaries
+ * whose structural zeros double-float cannot resolve (errors up to 1e-3); declare the charges
+ * (tnsp_lattice_charges) or use TNSP_FP64.
  */
 int tnsp_chains_init(tnsp_ctx* ctx, int B, const int32_t* configs, const uint64_t* seeds, int discard,
                      int precision);
+
+/* options of tnsp_set_option */
+#define TNSP_OPT_JACOBI_SWEEPS 1  /* sweep limit of the one-sided Jacobi SVD (default 60, range 1..1000);
+                                     a factorisation that does not converge within it sets
+                                     TNSP_ST_SVD_NOCONV and the call returns TNSP_E_DEVICE */
+#define TNSP_OPT_BLOCKS_PER_SM 2  /* resident sampler blocks per SM (0 = the most the occupancy
+                                     calculator allows, the default); fewer blocks give each chain's
+                                     block more shared memory for its factorisations */
+
+/*
+ * Sets a context option (TNSP_OPT_*).  Takes effect at the next tnsp_chains_init / tnsp_sweep.  A new
+ * TNSP_OPT_BLOCKS_PER_SM re-plans the per-block scratch, which drops the gradient sums accumulated since
+ * the last tnsp_observer_reset: set it before observing.
+ * Replaces: the reference's LAPACK error branch of the SVD (TAT/include/TAT/implement/svd.hpp:114-122,
+ * `what_if_lapack_error`), whose iteration limit is LAPACK's own; no counterpart for the block count.
+ */
+int tnsp_set_option(tnsp_ctx* ctx, int option, int value);
 
 /*
  * Runs `nsweeps` sweeps of every chain.  When `observe` is non-zero every sweep is followed by
@@ -202,18 +225,24 @@ int tnsp_last_timing(tnsp_ctx* ctx, double* ms, int64_t* launches);
 int tnsp_counters_read(tnsp_ctx* ctx, double* flops, int reset);
 
 /*
- * Allocation-free variant of tnsp_amplitude, for callers that cannot call cudaMalloc (code
- * running inside a CUDA-graph capture or a stream callback, processes whose device memory belongs
- * to a caching allocator, hosts that forbid allocation after start-up).  No counterpart in the
- * reference.  It needs no context: tensors (dense A[p][u][d][l][r], float64), configs
- * (B x L1*L2 int32), mantissa (B doubles) and exponent (B int32) are caller-owned DEVICE
- * pointers; dims (L1*L2*4 ints, as in tnsp_lattice_upload) is a host pointer; stream is a
- * cudaStream_t or NULL.  Configuration entries must lie in [0, P): they are not checked on the device.
- * The call is synchronous with respect to `stream`.
+ * Allocation-free variant of tnsp_amplitude.  No counterpart in the reference.  It is for callers that
+ * must not allocate device memory after start-up: a host application whose device memory is all
+ * reserved by its own pool or caching allocator (a cudaMalloc behind its back fails or fragments that
+ * pool), and latency-bound or real-time hosts, where cudaMalloc/cudaFree can synchronise the device
+ * and take unbounded time.  It needs no context: tensors (dense A[p][u][d][l][r], float64), configs
+ * (B x L1*L2 int32), mantissa (B doubles) and exponent (B int32) are caller-owned DEVICE pointers;
+ * dims (L1*L2*4 ints, as in tnsp_lattice_upload) is a host pointer; stream is a cudaStream_t or NULL.
+ * Configuration entries must lie in [0, P): they are not checked on the device.  The call returns
+ * after the stream has finished its work (it reads the device status word back).
+ * Every matrix is factorised as one block (no charge sectors are declared): for block-sparse tensors
+ * passed densely the amplitudes equal tnsp_amplitude's in float64 to rounding, at a higher cost.
  * Scratch comes from a 64 MiB array compiled into the library (held by every device that loads
- * it); a lattice/cut whose one-chain scratch does not fit returns TNSP_E_TOO_LARGE.  The first
- * call on a device resolves the array's address (cudaGetSymbolAddress): make it before any stream
- * capture.  Calls share the array: calls that overlap on the GPU race and must be serialised.
+ * it, until the process exits); cut * max bond extent above 1024, or a lattice/cut whose one-chain
+ * scratch does not fit in it, returns TNSP_E_TOO_LARGE before any device work.  The first call on a
+ * device resolves the array's device address (cudaGetSymbolAddress) with that device current: make
+ * that first call before any stream capture begins.  All calls share the array, which keeps the last
+ * call's contents (each call rewrites what must start at a known value): calls that overlap on the
+ * GPU race and must be serialised.  On failure tnsp_last_error(NULL) gives the reason.
  */
 int tnsp_amplitude_noalloc(int L1, int L2, int P, const int* dims, const double* tensors, int cut, int B,
                            const int32_t* configs, double* mantissa, int32_t* exponent, void* stream);

@@ -8,9 +8,10 @@
 # BLAS/LAPACK comes from scipy's bundled OpenBLAS, whose Fortran symbols carry a `scipy_` prefix;
 # -D aliases map TAT's extern "C" names onto them.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default: $TNSP_REFERENCE_ROOT)
 set -euo pipefail
-REF=${1:-/root/reference}
+REF=${1:-${TNSP_REFERENCE_ROOT:-}}
+if [ -z "$REF" ]; then echo "usage: $0 REFERENCE_ROOT (or set TNSP_REFERENCE_ROOT)" >&2; exit 2; fi
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 GEN="$OUT/gen"

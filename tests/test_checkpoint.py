@@ -72,10 +72,11 @@ def test_set_tensors_rejects_entries_outside_the_blocks():
 
 
 def _reference_modules():
-    """The reference's TAT / tetragono where this checkout has them (built by oracle/build_ref.sh)."""
-    ref_dir = "/root/reference"
+    """The reference's TAT / tetragono where this checkout has them: the reference tree named by
+    TNSP_REFERENCE_ROOT and its CPU module built by oracle/build_ref.sh."""
+    ref_dir = os.environ.get("TNSP_REFERENCE_ROOT", "")
     tat_dir = os.path.join(ROOT, "oracle", "_ref")
-    if not (os.path.isdir(os.path.join(ref_dir, "tetragono")) and os.path.isdir(tat_dir)
+    if not (ref_dir and os.path.isdir(os.path.join(ref_dir, "tetragono")) and os.path.isdir(tat_dir)
             and any(f.startswith("TAT") and f.endswith(".so") for f in os.listdir(tat_dir))):
         pytest.skip("the reference is not available in this checkout")
     sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))

@@ -73,3 +73,48 @@ def test_zero_amplitude_is_recorded_not_fatal():
     assert m[0] == 0.0
     s.sweep(1)
     assert s.status() & 8  # TNSP_ST_ZERO_WS
+
+
+def test_double_float_refused_for_uncharged_block_sparse_tensors():
+    """Block-sparse tensors passed densely without their charges lose precision in double-float
+    (rank-deficient boundaries): the library refuses the combination instead of returning wrong
+    values, and accepts the same tensors with the charges declared, or in float64."""
+    from golden_cases import Golden
+    from test_gpu_parity import make_lattice
+    from tnsp_gb300.engine import Sampler, TnspError
+    g = Golden("heis_u1_4x4_D111_dc5")
+    seeds = np.array(g.meta["chain_seeds"], dtype=np.uint64)
+    s = Sampler(make_lattice(g, charged=False), g.cut)
+    with pytest.raises(TnspError, match="double-float needs the charges"):
+        s.init_chains(g.neel(), seeds, precision="dd")
+    s.init_chains(g.neel(), seeds, precision="fp64")
+    Sampler(make_lattice(g, charged=True), g.cut).init_chains(g.neel(), seeds, precision="dd")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "dd"])
+def test_jacobi_sweep_limit_reports_a_device_failure(precision):
+    """A one-sided Jacobi SVD that does not converge within its sweep limit (here set to 1) sets
+    TNSP_ST_SVD_NOCONV, and the sweep returns TNSP_E_DEVICE with the status in its message, as the
+    reference raises on a LAPACK failure (TAT/include/TAT/implement/svd.hpp:114-122); the loop ends at
+    the limit, the context stays usable and the default limit gives the reference's chains again."""
+    from golden_cases import Golden
+    from test_gpu_parity import make_lattice
+    from tnsp_gb300 import _lib
+    from tnsp_gb300.engine import Sampler, TnspError
+    g = Golden("heis_no_4x4_D4_dc16")
+    seeds = np.array(g.meta["chain_seeds"], dtype=np.uint64)
+    s = Sampler(make_lattice(g), g.cut)
+    s.set_option(_lib.TNSP_OPT_JACOBI_SWEEPS, 1)
+    s.init_chains(g.neel(), seeds, precision=precision)
+    with pytest.raises(TnspError, match=r"\(-4\).*device status 0x"):
+        s.sweep(1)
+    assert s.status() & 1  # TNSP_ST_SVD_NOCONV (read and cleared)
+    with pytest.raises(TnspError, match="out of range"):
+        s.set_option(_lib.TNSP_OPT_JACOBI_SWEEPS, 0)
+    s.set_option(_lib.TNSP_OPT_JACOBI_SWEEPS, 60)
+    s.init_chains(g.neel(), seeds, precision=precision)
+    s.sweep(1)
+    conf, _ = s.read_chains()
+    for b in range(len(seeds)):
+        np.testing.assert_array_equal(conf[b], g.z["confs"][b][0])
+    assert s.status() == 0

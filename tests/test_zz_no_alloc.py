@@ -1,5 +1,6 @@
-"""tnsp_amplitude_noalloc: the allocation-free amplitude entry point, for callers that cannot call
-cudaMalloc (graph capture, stream callbacks, memory owned by a caching allocator).  Its output is
+"""tnsp_amplitude_noalloc: the allocation-free amplitude entry point, for callers that must not
+allocate device memory once running (a host whose device memory is all reserved by its own pool or
+caching allocator, or a latency-bound host where cudaMalloc may synchronise the device).  Its output is
 checked against the regular entry point tnsp_amplitude, on two calls in a row with different
 lattices, so the second call also shows that the shared scratch arena is reset between calls.
 
@@ -62,12 +63,26 @@ def test_noalloc_amplitude_matches_regular_entry_point_twice():
         np.testing.assert_allclose(got, ref, rtol=1e-10, atol=0)
 
 
-def test_noalloc_rejects_problems_beyond_the_arena():
+def _too_large(L1, L2, D, cut):
+    """Calls the entry point on a lattice/cut it must refuse before any device work (the device
+    pointers are placeholders that a refused call never touches)."""
     from tnsp_gb300 import _lib
     from tnsp_gb300.lattice import random_heisenberg
     lib = _lib.load()
-    lat = random_heisenberg(12, 12, 8, seed=1)
+    lat = random_heisenberg(L1, L2, D, seed=1)
     dims = np.ascontiguousarray(lat.dims())
-    rc = lib.tnsp_amplitude_noalloc(12, 12, 2, _lib.ptr(dims, ctypes.c_int), ctypes.c_void_p(16), 256, 1,
+    rc = lib.tnsp_amplitude_noalloc(L1, L2, 2, _lib.ptr(dims, ctypes.c_int), ctypes.c_void_p(16), cut, 1,
                                     ctypes.c_void_p(16), ctypes.c_void_p(16), ctypes.c_void_p(16), None)
-    assert rc == -6  # TNSP_E_TOO_LARGE, returned before any device work
+    return rc, lib.tnsp_last_error(None).decode()
+
+
+def test_noalloc_rejects_a_bond_dimension_beyond_its_limit():
+    rc, msg = _too_large(12, 12, 8, 256)   # cut * D = 2048 > 1024
+    assert rc == -6, msg                   # TNSP_E_TOO_LARGE
+    assert "1024" in msg
+
+
+def test_noalloc_rejects_a_chain_slot_beyond_the_arena():
+    rc, msg = _too_large(16, 16, 8, 128)   # cut * D = 1024 is allowed, but one chain slot exceeds 64 MiB
+    assert rc == -6, msg
+    assert "64 MiB" in msg

@@ -12,6 +12,8 @@ LIB_PATH = os.path.join(HERE, "libtnsp_gb300.so")
 TNSP_FP64 = 0
 TNSP_FP32 = 1
 TNSP_DD = 2
+TNSP_OPT_JACOBI_SWEEPS = 1
+TNSP_OPT_BLOCKS_PER_SM = 2
 PRECISIONS = {"fp64": TNSP_FP64, "fp32": TNSP_FP32, "dd": TNSP_DD}
 
 _c_int_p = ctypes.POINTER(ctypes.c_int)
@@ -47,6 +49,7 @@ SIGNATURES = {
     "tnsp_model_upload": (ctypes.c_int,
                           [_c_void_p, ctypes.c_int, _c_int_p, _c_int_p, _c_int_p, ctypes.c_int, _c_int_p, _c_dbl_p]),
     "tnsp_chains_init": (ctypes.c_int, [_c_void_p, ctypes.c_int, _c_i32_p, _c_u64_p, ctypes.c_int, ctypes.c_int]),
+    "tnsp_set_option": (ctypes.c_int, [_c_void_p, ctypes.c_int, ctypes.c_int]),
     "tnsp_sweep": (ctypes.c_int, [_c_void_p, ctypes.c_int, ctypes.c_int]),
     "tnsp_observer_reset": (ctypes.c_int, [_c_void_p]),
     "tnsp_observer_read": (ctypes.c_int, [_c_void_p, _c_dbl_p, _c_dbl_p, _c_dbl_p]),

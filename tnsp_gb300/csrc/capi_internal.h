@@ -84,11 +84,18 @@ struct tnsp_ctx {
   int* d_tfl = nullptr;
   int* d_ilist = nullptr;
   size_t smem_bytes = 0;
+  // options (tnsp_set_option)
+  int jacobi_max = tnsp::kMaxSweepsJacobi;  // sweep limit of the one-sided Jacobi SVD
+  int blocks_per_sm = 0;                    // resident sampler blocks per SM (0: the occupancy limit)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0;
   long long last_launches = 0;
 };
 
+
+// message of the calling thread's last failed tnsp_amplitude_noalloc call (noalloc.cu); returned by
+// tnsp_last_error(NULL)
+const char* tnsp_noalloc_error();
 
 namespace tnsp {
 

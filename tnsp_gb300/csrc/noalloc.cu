@@ -1,12 +1,13 @@
 // tnsp_amplitude_noalloc: the amplitude hole(()) of a batch of configurations without any
 // device allocation.
 //
-// Who needs it: callers that cannot call cudaMalloc -- code running inside a CUDA-graph capture
-// or another library's stream callback, processes whose device memory is entirely owned by a
-// caching allocator they must not bypass, and embedded hosts that forbid allocation after start-up.
-// The regular entry points allocate their per-chain scratch slots with cudaMalloc; this one takes
-// every input and output as a caller-owned device pointer and uses a fixed scratch arena compiled
-// into the library instead.
+// Who needs it: callers that must not allocate device memory once they are running -- a host
+// application whose device memory is all reserved by its own pool or caching allocator (a
+// cudaMalloc behind the allocator's back fails or fragments the pool), and latency-bound or
+// real-time hosts, where cudaMalloc and cudaFree can synchronise the device and take unbounded
+// time.  The regular entry points allocate their per-chain scratch slots with cudaMalloc; this one
+// takes every input and output as a caller-owned device pointer and uses a fixed scratch arena
+// compiled into the library instead.
 //
 // The arena is a file-scope __device__ array of kNoAllocArenaBytes (64 MiB).  Every GPU that loads
 // the library holds it until the process exits.  A problem whose scratch (metadata plus one
@@ -15,13 +16,16 @@
 // Sharing: all calls on a device use the same arena, and it keeps the contents of the last call.
 // Everything that must start at a known value (status word, the all-ones boundary element, site
 // metadata, the all-zero charges: this entry point treats every matrix as one block) is rewritten
-// by every call before the kernel runs.  Two calls whose work overlaps on
-// the GPU (different streams, or different host threads) race on the arena and give undefined
-// results: serialise them.
+// by every call before the kernel runs.  Two calls whose work overlaps on the GPU (different
+// streams, or different host threads) race on the arena and give undefined results: serialise them.
 //
 // Set-up: the first call on each device resolves the arena's device address with
 // cudaGetSymbolAddress (with that device current) and caches it; make that first call before any
-// stream capture begins.
+// stream capture begins.  The call itself copies small host arrays to the arena and waits for its
+// stream before it returns.
+//
+// Errors: the reason of the calling thread's last failure is kept in a thread-local buffer and is
+// returned by tnsp_last_error(NULL).
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -64,13 +68,26 @@ static cudaError_t arena_for_current_device(unsigned char** out) {
 
 static size_t align256(size_t n) { return (n + 255) / 256 * 256; }
 
+static thread_local char g_err[160] = "";
+
+// records the reason of a failure for tnsp_last_error(NULL) and returns its code
+static int fail(int code, const char* what, cudaError_t e = cudaSuccess) {
+  if (e != cudaSuccess)
+    snprintf(g_err, sizeof g_err, "tnsp_amplitude_noalloc: %s (%s)", what, cudaGetErrorString(e));
+  else
+    snprintf(g_err, sizeof g_err, "tnsp_amplitude_noalloc: %s", what);
+  return code;
+}
+
 }  // namespace tnsp_noalloc
+
+const char* tnsp_noalloc_error() { return tnsp_noalloc::g_err; }
 
 extern "C" int tnsp_amplitude_noalloc(int L1, int L2, int P, const int* dims, const double* tensors, int cut, int B,
                                       const int32_t* configs, double* mantissa, int32_t* exponent, void* stream) {
   using namespace tnsp;
   using namespace tnsp_noalloc;
-  auto err = [](int code, const char*) { return code; };  // the second argument documents the cause
+  auto err = [](int code, const char* what, cudaError_t e = cudaSuccess) { return fail(code, what, e); };
   if (L1 < 1 || L2 < 1 || L1 > kMaxL || L2 > kMaxL) return err(TNSP_E_ARG, "lattice extent out of range (1..16)");
   if (P < 1 || cut < 1 || B < 1) return err(TNSP_E_ARG, "P, cut and B must be positive");
   if (!dims || !tensors || !configs || !mantissa || !exponent) return err(TNSP_E_ARG, "null pointer argument");
@@ -124,7 +141,7 @@ extern "C" int tnsp_amplitude_noalloc(int L1, int L2, int P, const int* dims, co
     nslots = 4 * sms;
   unsigned char* base = nullptr;
   cudaError_t e = arena_for_current_device(&base);
-  if (e != cudaSuccess) return err(TNSP_E_CUDA, "cudaGetSymbolAddress failed");
+  if (e != cudaSuccess) return err(TNSP_E_CUDA, "cudaGetSymbolAddress failed", e);
   cudaStream_t st = (cudaStream_t)stream;
   size_t o = 0;
   auto carve = [&](size_t bytes) {
@@ -160,7 +177,7 @@ extern "C" int tnsp_amplitude_noalloc(int L1, int L2, int P, const int* dims, co
       (e = cudaMemsetAsync(d_qleg, 0, sizeof(int) * (size_t)ns * 4 * Dmax, st)) != cudaSuccess ||
       (e = cudaMemsetAsync(d_qphys, 0, sizeof(int) * (size_t)P, st)) != cudaSuccess ||
       (e = cudaMemsetAsync(d_sflux, 0, sizeof(int) * (size_t)ns, st)) != cudaSuccess)
-    return err(TNSP_E_CUDA, "arena set-up copy failed");
+    return err(TNSP_E_CUDA, "arena set-up copy failed", e);
   Model md{};
   md.L1 = L1;
   md.L2 = L2;
@@ -174,12 +191,18 @@ extern "C" int tnsp_amplitude_noalloc(int L1, int L2, int P, const int* dims, co
   md.qleg = d_qleg;
   md.qphys = d_qphys;
   md.sflux = d_sflux;
+  md.jacobi_max = kMaxSweepsJacobi;
   launch_amplitude_f64(nslots, 0, st, md, s, d_scratch, d_ones, B, configs, mantissa, exponent, d_status);
-  if ((e = cudaGetLastError()) != cudaSuccess) return err(TNSP_E_CUDA, "kernel launch failed");
+  if ((e = cudaGetLastError()) != cudaSuccess) return err(TNSP_E_CUDA, "kernel launch failed", e);
   int32_t status = 0;
   if ((e = cudaMemcpyAsync(&status, d_status, sizeof(int32_t), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
       (e = cudaStreamSynchronize(st)) != cudaSuccess)
-    return err(TNSP_E_CUDA, "stream synchronisation failed");
-  if (status & (TNSP_ST_SVD_NOCONV | TNSP_ST_NONFINITE)) return err(TNSP_E_DEVICE, "device status word set");
+    return err(TNSP_E_CUDA, "stream synchronisation failed", e);
+  if (status & (TNSP_ST_SVD_NOCONV | TNSP_ST_NONFINITE)) {
+    char buf[96];
+    snprintf(buf, sizeof buf, "device status 0x%x (see TNSP_ST_* bits)", status);
+    return err(TNSP_E_DEVICE, buf);
+  }
+  g_err[0] = 0;
   return TNSP_OK;
 }

@@ -27,7 +27,7 @@ namespace tnsp {
 constexpr int kMaxL = 16;       // lattice extent limit (rows or columns)
 constexpr int kMaxSites = kMaxL * kMaxL;
 constexpr int kMtN = 312;
-constexpr int kMaxSweepsJacobi = 60;
+constexpr int kMaxSweepsJacobi = 60;   // default sweep limit of the one-sided Jacobi SVD
 constexpr int kMaxSec = 96;     // charge sectors per factorised matrix
 constexpr int kMaxChi = 1024;   // cut * Dmax
 constexpr int kCounters = 16;   // per-slot counters: 4 flop classes + 12 phase cycle counters
@@ -65,6 +65,7 @@ struct Model {
   int fermion;
   int pT;                   // parity of the T leg's charge
   const long long* poff;
+  int jacobi_max;           // sweep limit of the one-sided Jacobi SVD
 };
 
 struct Chains {
@@ -840,8 +841,8 @@ template <class T> struct Engine : Chain<T> {
       }
       toc(PH_SVDOUT, t0);  // gather + pivoted QR
       t0 = tic();
-      const int sweeps = ns == 1 ? block_jacobi(s_nvv[0], s_nvv[0], s_bp[0], s_jp[0], kMaxSweepsJacobi)
-                                 : block_jacobi_multi<T, kMaxSec>(ns, s_nvv, s_nvv, s_bp, s_jp, kMaxSweepsJacobi);
+      const int sweeps = ns == 1 ? block_jacobi(s_nvv[0], s_nvv[0], s_bp[0], s_jp[0], md.jacobi_max)
+                                 : block_jacobi_multi<T, kMaxSec>(ns, s_nvv, s_nvv, s_bp, s_jp, md.jacobi_max);
       toc(PH_JACOBI, t0);
       t0 = tic();
       if (sweeps < 0 && threadIdx.x == 0) atomicOr(status, ST_SVD_NOCONV);

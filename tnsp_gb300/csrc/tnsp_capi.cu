@@ -194,6 +194,7 @@ Model make_model(tnsp_ctx* c) {
   m.qleg = c->d_qleg;
   m.qphys = c->d_qphys;
   m.sflux = c->d_sflux;
+  m.jacobi_max = c->jacobi_max;
   return m;
 }
 
@@ -225,8 +226,13 @@ int ensure_slots(tnsp_ctx* ctx) {
   ctx->elem = ctx->precision == TNSP_FP32 ? 4 : 8;
   // dynamic shared memory for sector staging.  Per block: 56 KB + ~15 KB static + 1 KB reserved, so
   // three blocks fit in an SM's 228 KB (64 KB allowed only two); the register budget of the sweep
-  // kernel (168 per thread) also allows three 128-thread blocks.
+  // kernel (168 per thread) also allows three 128-thread blocks.  With TNSP_OPT_BLOCKS_PER_SM = b the
+  // SM's shared memory is split b ways instead (fewer chains at once, larger sectors staged on chip).
   ctx->smem_bytes = 56 * 1024;
+  if (ctx->blocks_per_sm > 0) {
+    const long long share = 228LL * 1024 / ctx->blocks_per_sm - 20LL * 1024;  // static + reserved margin
+    ctx->smem_bytes = (size_t)std::max(0LL, std::min(200LL * 1024, share / 1024 * 1024));
+  }
   int occ = 0;
   if (ctx->precision == TNSP_FP64) {
     CK(set_smem_limit_f64((int)ctx->smem_bytes));
@@ -238,6 +244,9 @@ int ensure_slots(tnsp_ctx* ctx) {
     CK(set_smem_limit_f32((int)ctx->smem_bytes));
     CK(occupancy_f32((int)ctx->smem_bytes, &occ));
   }
+  if (ctx->blocks_per_sm > 0 && occ < ctx->blocks_per_sm)
+    return fail(ctx, TNSP_E_ARG, "TNSP_OPT_BLOCKS_PER_SM exceeds the blocks an SM can hold for this kernel");
+  if (ctx->blocks_per_sm > 0) occ = ctx->blocks_per_sm;
   // one resident wave of blocks (the occupancy limit per SM), bounded by a scratch budget of 64 GB
   long long want = (long long)std::max(1, occ) * sms;
   const long long per = s.stride * (long long)ctx->elem + 2LL * ctx->n_params * 8;
@@ -353,7 +362,28 @@ int tnsp_ctx_destroy(tnsp_ctx* ctx) {
   return TNSP_OK;
 }
 
-const char* tnsp_last_error(tnsp_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+const char* tnsp_last_error(tnsp_ctx* ctx) { return ctx ? ctx->err.c_str() : tnsp_noalloc_error(); }
+
+int tnsp_set_option(tnsp_ctx* ctx, int option, int value) {
+  if (!ctx) return TNSP_E_ARG;
+  switch (option) {
+    case TNSP_OPT_JACOBI_SWEEPS:
+      if (value < 1 || value > 1000) return fail(ctx, TNSP_E_ARG, "Jacobi sweep limit out of range (1..1000)");
+      ctx->jacobi_max = value;
+      return TNSP_OK;
+    case TNSP_OPT_BLOCKS_PER_SM:
+      if (value < 0 || value > 32) return fail(ctx, TNSP_E_ARG, "blocks per SM out of range (0..32)");
+      if (value != ctx->blocks_per_sm) {
+        CK(cudaSetDevice(ctx->device));
+        CK(cudaDeviceSynchronize());
+        free_slots(ctx);  // re-planned at the next use
+        ctx->blocks_per_sm = value;
+      }
+      return TNSP_OK;
+    default:
+      return fail(ctx, TNSP_E_ARG, "unknown option");
+  }
+}
 
 int tnsp_lattice_upload(tnsp_ctx* ctx, int L1, int L2, int P, const int* dims, const double* tensors, int cut) {
   if (!ctx) return TNSP_E_ARG;
@@ -586,6 +616,20 @@ int tnsp_chains_init(tnsp_ctx* ctx, int B, const int32_t* configs, const uint64_
   const int ns = ctx->L1 * ctx->L2;
   for (long long i = 0; i < (long long)B * ns; ++i)
     if (configs[i] < 0 || configs[i] >= ctx->P) return fail(ctx, TNSP_E_ARG, "configuration index out of range");
+  if (precision == TNSP_DD && !ctx->charged) {
+    // block-sparse tensors passed densely without their charges: the structural zeros make
+    // rank-deficient boundaries that double-float resolves only to ~1e-3 (float64 is exact there)
+    for (int id = 0; id < ns; ++id) {
+      const long long n = (id + 1 < ns ? ctx->off[id + 1] : ctx->n_params) - ctx->off[id];
+      long long zeros = 0;
+      for (long long i = 0; i < n; ++i) zeros += ctx->hostA[ctx->off[id] + i] == 0.0;
+      if (4 * zeros > n)
+        return fail(ctx, TNSP_E_ARG,
+                    "double-float needs the charges of block-sparse tensors: site " + std::to_string(id) +
+                        " is more than a quarter exact zeros and no charges were declared (call "
+                        "tnsp_lattice_charges, or use TNSP_FP64)");
+    }
+  }
   CK(cudaSetDevice(ctx->device));
   if (B != ctx->B || precision != ctx->precision) {
     free_chains(ctx);

@@ -80,6 +80,10 @@ class Sampler:
             self._static_uploaded = True
         self._uploaded_version = lat.version
 
+    def set_option(self, option, value):
+        """A context option (``_lib.TNSP_OPT_JACOBI_SWEEPS`` / ``_lib.TNSP_OPT_BLOCKS_PER_SM``)."""
+        self._check(self.lib.tnsp_set_option(self.ctx, int(option), int(value)), "tnsp_set_option")
+
     def init_chains(self, configs, seeds, discard=0, precision=TNSP_FP64):
         """``precision``: TNSP_FP64 / TNSP_FP32 / TNSP_DD or one of "fp64", "fp32", "dd"."""
         if isinstance(precision, str):
