@@ -91,23 +91,29 @@ def phase_share(cycles):
     return {n: c / tot for n, c in timed.items() if c > 0}
 
 
-def tau_int(series):
-    """Integrated autocorrelation time of E_loc; series shape (n_samples, n_chains)."""
+def tau_int(series, window=5.0):
+    """Integrated autocorrelation time of E_loc from independent chains; ``series`` has shape
+    (n_samples, n_chains).  Each chain's own mean is subtracted, the autocovariance at lag t is pooled
+    over chains (sum over chains and over the n - t pairs of each) and normalised by the pooled
+    lag-0 variance, and the sum 1/2 + sum_t rho(t) is cut by Sokal's automatic window (the first
+    t >= window * tau(t)).  Returns (tau, details); tau is floored at 1/2 (independent samples)."""
     x = np.asarray(series, dtype=np.float64)
-    n = x.shape[0]
+    if x.ndim == 1:
+        x = x[:, None]
+    n, c = x.shape
     if n < 3:
-        return 0.5
-    x = x - x.mean()
-    var = (x * x).mean()
+        return 0.5, {"n_per_chain": int(n), "chains": int(c), "window": 0, "raw": None}
+    x = x - x.mean(axis=0, keepdims=True)
+    var = (x * x).sum() / (n * c)
     if var <= 0:
-        return 0.5
-    tau = 0.5
-    for t in range(1, n // 2):
-        rho = (x[:-t] * x[t:]).mean() / var
+        return 0.5, {"n_per_chain": int(n), "chains": int(c), "window": 0, "raw": None}
+    tau, t = 0.5, 0
+    for t in range(1, n - 1):
+        rho = (x[:-t] * x[t:]).sum() / ((n - t) * c) / var
         tau += rho
-        if t >= 5 * tau:
+        if t >= window * tau:
             break
-    return max(tau, 0.5)
+    return max(tau, 0.5), {"n_per_chain": int(n), "chains": int(c), "window": int(t), "raw": float(tau)}
 
 
 # ---------------------------------------------------------------------------------------------
@@ -148,7 +154,7 @@ def cpu_baseline(workload, seconds, cores=None):
     busy = max(r[1] for r in res)
     m = min(len(r[2]) for r in res)
     series = np.array([r[2][:m] for r in res]).T if m > 0 else np.zeros((0, cores))
-    return dict(samples=n, seconds=busy, wall=wall, cores=cores, tau=tau_int(series) if m >= 3 else None)
+    return dict(samples=n, seconds=busy, wall=wall, cores=cores, tau=tau_int(series)[0] if m >= 3 else None)
 
 
 # ---------------------------------------------------------------------------------------------
@@ -300,7 +306,7 @@ def run_ours(args):
     if dist:
         t_e2e = reduce_over_ranks(dist, t_e2e, "max", "cuda")
     series = np.array(warm_eloc + elocs)
-    tau = tau_int(series)
+    tau, tau_info = tau_int(series)
     samples = B * args.steps * world
     raw = samples / t_dev
     value = raw / (2 * tau)

@@ -43,6 +43,19 @@ import numpy as np
 
 from .rng import MT19937_64, uniform_int, uniform_real01
 
+# Every tensor contraction of the boundary-MPS path goes through these three functions (float64 by
+# default).  oracle/precision_study.py replaces them to measure what lower-precision products (float32,
+# split TF32/BF16 products with float32 accumulation) do to amplitudes and E_loc, with the QR and SVD
+# kept in float64.
+contract = np.tensordot
+matmul = np.matmul
+
+
+def full_dot(a, b):
+    """sum of a * b over all (three) legs"""
+    return np.einsum("arb,arb->", a, b)
+
+
 
 # ----------------------------------------------------------------------------------------------
 # boundary MPS
@@ -81,7 +94,7 @@ def compress(line, sites, cut, line_q=None, site_q=None):
         a, p, b = line[i].shape
         u, d, l, r = sites[i].shape
         assert p == u
-        t = np.tensordot(line[i], sites[i], axes=([1], [0]))  # (a, b, d, l, r)
+        t = contract(line[i], sites[i], axes=([1], [0]))  # (a, b, d, l, r)
         T.append(t.transpose(0, 3, 2, 1, 4).reshape(a * l, d, b * r))
         la, lb, lf = line_q[i] if line_q is not None else (np.zeros(a, int), np.zeros(b, int), 0)
         _, sd, sl, sr, sf = site_q[i] if site_q is not None else (None, np.zeros(d, int), np.zeros(l, int),
@@ -110,7 +123,7 @@ def compress(line, sites, cut, line_q=None, site_q=None):
             k0 += k
         T[i] = Q.reshape(A, d, ktot)
         b_, d_, c_ = T[i + 1].shape
-        T[i + 1] = (R @ T[i + 1].reshape(b_, d_ * c_)).reshape(ktot, d_, c_)
+        T[i + 1] = matmul(R, T[i + 1].reshape(b_, d_ * c_)).reshape(ktot, d_, c_)
         qB[i] = -qk
         qA[i + 1] = qk
         F[i + 1] += F[i]
@@ -139,7 +152,7 @@ def compress(line, sites, cut, line_q=None, site_q=None):
             qk[t] = r
         T[i] = Vnew.reshape(c, d, B)
         a_, d_, b_ = T[i - 1].shape
-        T[i - 1] = (T[i - 1].reshape(a_ * d_, b_) @ US).reshape(a_, d_, c)
+        T[i - 1] = matmul(T[i - 1].reshape(a_ * d_, b_), US).reshape(a_, d_, c)
         qA[i] = qk
         qB[i - 1] = -qk
     return T, [(qA[i], qB[i], F[i]) for i in range(n)]
@@ -150,16 +163,16 @@ def compress(line, sites, cut, line_q=None, site_q=None):
 # ----------------------------------------------------------------------------------------------
 def strip_step_left(E, up, site, down):
     """E (x, y, z) -> E' (a, r, b): absorb one column of a three-line strip from the left."""
-    t1 = np.tensordot(E, up, axes=([0], [0]))  # (y, z, u, a)
-    t2 = np.tensordot(t1, site, axes=([0, 2], [2, 0]))  # (z, a, d, r)
-    return np.tensordot(t2, down, axes=([0, 2], [0, 1]))  # (a, r, b)
+    t1 = contract(E, up, axes=([0], [0]))  # (y, z, u, a)
+    t2 = contract(t1, site, axes=([0, 2], [2, 0]))  # (z, a, d, r)
+    return contract(t2, down, axes=([0, 2], [0, 1]))  # (a, r, b)
 
 
 def strip_step_right(F, up, site, down):
     """F (a, r, b) -> F' (x, l, z): absorb one column of a three-line strip from the right."""
-    s1 = np.tensordot(up, F, axes=([2], [0]))  # (x, u, r, b)
-    s2 = np.tensordot(s1, site, axes=([1, 2], [0, 3]))  # (x, b, d, l)
-    return np.tensordot(s2, down, axes=([1, 2], [2, 1])).transpose(0, 1, 2)  # (x, l, z)
+    s1 = contract(up, F, axes=([2], [0]))  # (x, u, r, b)
+    s2 = contract(s1, site, axes=([1, 2], [0, 3]))  # (x, b, d, l)
+    return contract(s2, down, axes=([1, 2], [2, 1])).transpose(0, 1, 2)  # (x, l, z)
 
 
 def strip_envs(up, sites, down):
@@ -184,9 +197,9 @@ def strip_value(up, sites, down):
 
 def strip_hole(E_left, up, down, F_right):
     """d value / d site, shape (u, d, l, r)."""
-    h1 = np.tensordot(E_left, up, axes=([0], [0]))  # (l, z, u, a)
-    h2 = np.tensordot(h1, down, axes=([1], [0]))  # (l, u, a, d, b)
-    h = np.tensordot(h2, F_right, axes=([2, 4], [0, 2]))  # (l, u, d, r)
+    h1 = contract(E_left, up, axes=([0], [0]))  # (l, z, u, a)
+    h2 = contract(h1, down, axes=([1], [0]))  # (l, u, a, d, b)
+    h = contract(h2, F_right, axes=([2, 4], [0, 2]))  # (l, u, d, r)
     return h.transpose(1, 2, 0, 3)
 
 
@@ -350,7 +363,7 @@ class Environment:
         up, down = self.up(l1 - 1), self.down(l1 + 1)
         e = strip_step_left(E[l2], up[l2], p.site(l1, l2, s0), down[l2])
         e = strip_step_left(e, up[l2 + 1], p.site(l1, l2 + 1, s1), down[l2 + 1])
-        return float(np.einsum("arb,arb->", e, F[l2 + 2]))
+        return float(full_dot(e, F[l2 + 2]))
 
     def replace_vertical(self, l1, l2, s0, s1):
         """psi with sites (l1,l2),(l1+1,l2) set to s0,s1 (single_layer_auxiliaries.py:686-692)."""
@@ -359,7 +372,7 @@ class Environment:
         lf, rt = self.left(l2 - 1), self.right(l2 + 1)
         e = strip_step_left(E[l1], lf[l1], p.site(l1, l2, s0).transpose(2, 3, 0, 1), rt[l1])
         e = strip_step_left(e, lf[l1 + 1], p.site(l1 + 1, l2, s1).transpose(2, 3, 0, 1), rt[l1 + 1])
-        return float(np.einsum("arb,arb->", e, F[l1 + 2]))
+        return float(full_dot(e, F[l1 + 2]))
 
     def site_hole(self, l1, l2):
         """d psi / d A[l1,l2][s] from the row strip, shape (u, d, l, r)."""

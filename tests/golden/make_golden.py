@@ -3,7 +3,7 @@
 Run in a container that has the reference checkout and the reference CPU build
 (``oracle/build_ref.sh``):
 
-    python tests/golden/make_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_golden.py [REFERENCE_ROOT]   (default: $TNSP_REFERENCE_ROOT)
 
 Each case builds a seeded random PEPS with the reference's own classes, runs independent sweep
 chains with ``SweepSampling`` and measures every sample with ``Observer`` (energy + gradient),
@@ -29,7 +29,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 _ARGS = [a for a in sys.argv[1:] if not a.startswith("--")]
-REF = _ARGS[0] if _ARGS else "/root/reference"
+REF = _ARGS[0] if _ARGS else os.environ.get("TNSP_REFERENCE_ROOT", "")
+if not REF and __name__ == "__main__":
+    sys.exit("usage: make_golden.py REFERENCE_ROOT (or set TNSP_REFERENCE_ROOT)")
 
 
 def install_mpi_stub():
@@ -171,15 +173,20 @@ def build_lattice(kind, L1, L2, D, seed):
     return lattice
 
 
-def run_case(name, kind, L1, L2, D, cut, tensor_seed, chain_seeds, n_therm, n_samples):
+def run_case(name, kind, L1, L2, D, cut, tensor_seed, chain_seeds, n_therm, n_samples, compact=False):
+    """``compact`` (the benchmark-size lattices): site tensors as block storage only (the dense form
+    follows from the edges), no per-sample holes, and the gradient as the values of its allowed
+    entries only (those where the dense site tensor is nonzero, in row-major order)."""
     lattice = build_lattice(kind, L1, L2, D, tensor_seed)
     out = {}
     meta = {"name": name, "kind": kind, "L1": L1, "L2": L2, "D": D, "cut": cut, "tensor_seed": tensor_seed,
-            "chain_seeds": chain_seeds, "n_therm": n_therm, "n_samples": n_samples, "sites": {}, "terms": []}
+            "chain_seeds": chain_seeds, "n_therm": n_therm, "n_samples": n_samples, "sites": {}, "terms": [],
+            "compact": compact}
     for l1 in range(L1):
         for l2 in range(L2):
             t = lattice[l1, l2]
-            out[f"site_{l1}_{l2}_dense"] = dense_site(t)
+            if not compact:
+                out[f"site_{l1}_{l2}_dense"] = dense_site(t)
             out[f"site_{l1}_{l2}_storage"] = np.array(t.storage).copy()
             meta["sites"][f"{l1},{l2}"] = edge_meta(t)
     phys = lattice.physics_edges[0, 0, 0]
@@ -220,12 +227,13 @@ def run_case(name, kind, L1, L2, D, cut, tensor_seed, chain_seeds, n_therm, n_sa
                     ws = float(configuration.hole(()).storage[0])
                     reweight = ws * ws / possibility
                     eloc = (observer._whole_result_reweight["energy"] - before) / reweight
-                    holes = configuration.holes()
                     c_ws.append(ws)
                     c_eloc.append(eloc)
-                    c_holes.append(np.stack([
-                        np.stack([dense_site(holes[l1][l2]) for l2 in range(L2)]) for l1 in range(L1)
-                    ]) if _same_shapes(holes, L1, L2) else _pack_holes(holes, L1, L2))
+                    if not compact:
+                        holes = configuration.holes()
+                        c_holes.append(np.stack([
+                            np.stack([dense_site(holes[l1][l2]) for l2 in range(L2)]) for l1 in range(L1)
+                        ]) if _same_shapes(holes, L1, L2) else _pack_holes(holes, L1, L2))
             confs.append(c_confs)
             poss.append(c_poss)
             ws_list.append(c_ws)
@@ -235,16 +243,23 @@ def run_case(name, kind, L1, L2, D, cut, tensor_seed, chain_seeds, n_therm, n_sa
     out["possibility"] = np.array(poss)
     out["ws"] = np.array(ws_list)
     out["eloc"] = np.array(eloc_list)
-    for l1 in range(L1):
-        for l2 in range(L2):
-            out[f"holes_{l1}_{l2}"] = np.array([[h[l1][l2] for h in c] for c in holes_list])
+    if not compact:
+        for l1 in range(L1):
+            for l2 in range(L2):
+                out[f"holes_{l1}_{l2}"] = np.array([[h[l1][l2] for h in c] for c in holes_list])
     energy, error = observer.energy
     out["energy"] = np.array([energy, error])
     out["total_weight"] = np.array(observer._total_weight)
     grad = observer.gradient
     for l1 in range(L1):
         for l2 in range(L2):
-            out[f"grad_{l1}_{l2}"] = dense_site(grad[l1][l2])
+            g = dense_site(grad[l1][l2])
+            if compact:
+                mask = dense_site(lattice[l1, l2]) != 0
+                assert not g[~mask].any()
+                out[f"grad_{l1}_{l2}_allowed"] = g[mask]
+            else:
+                out[f"grad_{l1}_{l2}"] = g
     meta["sweep_order"] = sweep_order
     out["meta"] = np.array(json.dumps(meta))
     path = os.path.join(HERE, f"{name}.npz")
@@ -397,6 +412,12 @@ def _pack_holes(holes, L1, L2):
     return [[dense_site(holes[l1][l2]) for l2 in range(L2)] for l1 in range(L1)]
 
 
+if __name__ == "__main__" and "--workloads" in sys.argv:
+    # the benchmark-size lattices: 8x8 Bose U(1) D=6 {-1:2, 0:2, +1:2} with Dcut 36, and 6x6 Bose U(1)
+    # D=4 {-1:1, 0:2, +1:1} with Dcut 16 (a few chains and sweeps each: seconds per sample here)
+    run_case("heis_u1_8x8_D222_dc36", "u1", 8, 8, (2, 2, 2), 36, 20260101, [101, 102], 2, 3, compact=True)
+    run_case("heis_u1_6x6_D121_dc16", "u1", 6, 6, (1, 2, 1), 16, 20260102, [111, 112], 3, 4, compact=True)
+    sys.exit(0)
 if __name__ == "__main__" and "--direct-only" in sys.argv:
     run_direct_case("heis_no_3x3_D3_dc4", "no", 3, 3, 3, 1234, 64, 256, [(5, 1.0, 12), (6, 0.5, 12)])
     run_direct_case("heis_no_3x3_D3_dc4_trunc", "no", 3, 3, 3, 1234, 4, 6, [(5, 1.0, 12), (6, 0.5, 12)])

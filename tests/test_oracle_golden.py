@@ -3,7 +3,7 @@ import os
 import numpy as np
 import pytest
 
-from golden_cases import CASES, GOLDEN, Golden
+from golden_cases import CASES, GOLDEN, WORKLOAD_CASES, Golden
 from oracle.peps_oracle import DensePEPS, ObserverAccumulator, SweepChain, sweep_order
 from oracle.rng import MT19937_64, uniform_int, uniform_real01
 
@@ -74,6 +74,36 @@ def test_oracle_matches_reference(name, charged):
     for l1 in range(g.L1):
         for l2 in range(g.L2):
             ref = z[f"grad_{l1}_{l2}"]
+            assert np.abs(grad[l1][l2] - ref).max() <= 1e-10 * max(1.0, np.abs(ref).max())
+
+
+@pytest.mark.parametrize("name", WORKLOAD_CASES)
+def test_oracle_matches_reference_on_benchmark_lattices(name):
+    """The oracle on the benchmark-size lattices (8x8 U(1) D=6 Dcut 36; 6x6 U(1) D=4 Dcut 16), where the
+    truncation keeps Dcut of up to D*Dcut singular values over many sectors: configurations bit-exact,
+    values to 1e-10 relative, the gradient on its allowed entries."""
+    g = Golden(name)
+    dense = g.dense_sites()
+    peps = DensePEPS(dense, g.terms(), g.cut, golden_charges(g))
+    acc = ObserverAccumulator(peps)
+    z = g.z
+    for ci, seed in enumerate(g.meta["chain_seeds"]):
+        chain = SweepChain(peps, g.neel(), seed)
+        for k in range(g.meta["n_therm"] + g.meta["n_samples"]):
+            poss, conf = chain.sweep()
+            np.testing.assert_array_equal(conf, z["confs"][ci][k])
+            assert abs(poss / z["possibility"][ci][k] - 1) < 1e-10
+            if k >= g.meta["n_therm"]:
+                j = k - g.meta["n_therm"]
+                ws, eloc, _ = acc.add(poss, conf, chain.env)
+                assert abs(ws / z["ws"][ci][j] - 1) < 1e-10
+                assert abs(eloc - z["eloc"][ci][j]) < 1e-10 * max(1.0, abs(z["eloc"][ci][j]))
+    e, err = acc.energy()
+    assert abs(e - z["energy"][0]) < 1e-12
+    grad = acc.gradient()
+    for l1 in range(g.L1):
+        for l2 in range(g.L2):
+            ref = g.gradient(l1, l2, dense)
             assert np.abs(grad[l1][l2] - ref).max() <= 1e-10 * max(1.0, np.abs(ref).max())
 
 
