@@ -227,7 +227,7 @@ def dist_setup(gpus):
 
 def run_ours(args):
     import torch
-    from tnsp_gb300.engine import PRECISIONS, Sampler, TNSP_DD, TNSP_FP32, TNSP_FP64
+    from tnsp_gb300.engine import PRECISIONS, Sampler, TNSP_DD, TNSP_FP32, TNSP_FP64, TNSP_MIXED
     from tnsp_gb300.lattice import neel
     rank, world, dist = dist_setup(args.gpus)
     local = int(os.environ.get("LOCAL_RANK", 0))
@@ -330,7 +330,7 @@ def run_ours(args):
     if prec == TNSP_FP64:
         bound, kname, peak = "fp64", "sweep_kernel<double>", FP64_NOMINAL_GFLOPS
         peak_src = "nominal GB300 FP64 1.25 TFLOP/s (MEASURED_PEAKS.json has no FP64 figure)"
-    elif prec == TNSP_DD:
+    elif prec in (TNSP_DD, TNSP_MIXED):
         bound, kname, peak = "fp32 (double-float)", "sweep_kernel<dd>", DD_NOMINAL_GFLOPS
         peak_src = (f"nominal GB300 FP32 {FP32_NOMINAL_GFLOPS:.0f} GFLOP/s / {DD_FMA_INSTRUCTIONS} FP32 instructions "
                     "per double-float multiply-add (MEASURED_PEAKS.json has no FP32 figure)")
@@ -359,7 +359,8 @@ def run_ours(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": {TNSP_FP64: "f64", TNSP_FP32: "f32", TNSP_DD: "f32x2 (double-float)"}[prec],
+        "dtype": {TNSP_FP64: "f64", TNSP_FP32: "f32", TNSP_DD: "f32x2 (double-float)",
+                  TNSP_MIXED: "f32 contractions, f32x2 (double-float) factorisations"}[prec],
         "data": "synthetic (seeded random PEPS, Neel start)",
         "config": {"workload": args.workload, "lattice": f"{w['L1']}x{w['L2']}", "D": w["D"],
                    "sectors": w["sectors"], "Dcut": w["cut"], "precision": args.precision, "chains_per_gpu": B,
@@ -446,7 +447,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="", choices=["", "fp64", "dd", "fp32"], help="default: per workload")
+    ap.add_argument("--precision", default="", choices=["", "fp64", "dd", "fp32", "mixed"], help="default: per workload")
     ap.add_argument("--chains", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")

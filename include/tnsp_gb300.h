@@ -38,10 +38,15 @@ typedef struct tnsp_ctx tnsp_ctx;
  *   TNSP_FP64  float64 (the reference's arithmetic)
  *   TNSP_FP32  float32; too coarse where amplitudes cancel strongly (large lattices)
  *   TNSP_DD    double-float: each value is a pair of floats (hi + lo, about 2^-46 relative
- *              precision) computed on the FP32 pipe, which GB300 runs at 64x its FP64 rate */
+ *              precision) computed on the FP32 pipe, which GB300 runs at 64x its FP64 rate
+ *   TNSP_MIXED the factorisations (per-sector QR and truncated SVD) in double-float, the tensors
+ *              (boundaries, compression tensors, strips) stored and contracted in float32; amplitudes
+ *              and E_loc carry float32-level rounding (~1e-5 relative on an 8x8 D=6 Dcut=36 lattice)
+ *              while the truncation decisions keep double-float precision */
 #define TNSP_FP64 0
 #define TNSP_FP32 1
 #define TNSP_DD 2
+#define TNSP_MIXED 3
 
 /*
  * Creates a context on CUDA device `device` using stream `stream` (a cudaStream_t, or NULL for
@@ -111,7 +116,7 @@ int tnsp_model_upload(tnsp_ctx* ctx, int n_terms, const int* sites, const int* o
  * seeds chain b's mt19937_64 exactly as TAT.random.seed does, and `discard` uniform_real draws
  * are skipped first (SeedDiffer draws one, tetragono/tetragono/utility.py:146-150).
  * Replaces: Configuration.import_configuration (lattice.py:181-206) + TAT.random.seed (PyTAT/PyTAT.hpp:89-94).
- * TNSP_DD is refused (TNSP_E_ARG) for a lattice uploaded without charges whose site tensors are more
+ * TNSP_DD and TNSP_MIXED are refused (TNSP_E_ARG) for a lattice uploaded without charges whose site tensors are more
  * than a quarter exact zeros: such block-sparse tensors stored densely make rank-deficient boundaries
  * whose structural zeros double-float cannot resolve (errors up to 1e-3); declare the charges
  * (tnsp_lattice_charges) or use TNSP_FP64.

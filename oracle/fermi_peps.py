@@ -335,6 +335,25 @@ def order_sign(conf, names_from, names_to, T_symmetry):
     return float(t.transpose(list(names_to)).scalar())
 
 
+def order_sign_by_count(conf, names_from, names_to, T_symmetry):
+    """``order_sign`` without building the tensor (any number of legs): a reordering of dimension-1
+    legs exchanges pairs of legs, and only pairs whose legs are both odd contribute a sign
+    (TAT/include/TAT/implement/edge_operator.hpp:521-555), so the sign is (-1)^(inversions among the
+    odd legs)."""
+    conf = np.asarray(conf)
+
+    def parity(n):
+        if n == "T":
+            return int(T_symmetry) & 1
+        return int(conf[int(n.split("_")[1]), int(n.split("_")[2])]) & 1
+
+    odd = [n for n in names_from if parity(n)]
+    pos = {n: i for i, n in enumerate(names_to)}
+    seq = [pos[n] for n in odd]
+    inv = sum(1 for i in range(len(seq)) for j in range(i + 1, len(seq)) if seq[i] > seq[j])
+    return -1.0 if inv & 1 else 1.0
+
+
 def hole_network(sites, conf, l1, l2):
     """``hole(((l1, l2),))`` exactly (single_layer_auxiliaries.py:721-736): every projected tensor but
     the one at (l1, l2), contracted; the bonds to (l1, l2) stay open, named as the reference names

@@ -56,7 +56,7 @@ def test_reduce_over_ranks_without_a_group_is_identity():
 
 def test_workloads_are_consistent():
     for name, w in bench.WORKLOADS.items():
-        assert w["precision"] in ("fp64", "dd", "fp32"), name
+        assert w["precision"] in ("fp64", "dd", "fp32", "mixed"), name
         assert w["chains"] >= 1 and w["steps"] >= 1
     assert bench.DEFAULT_WORKLOAD in bench.WORKLOADS
     assert abs(bench.DD_NOMINAL_GFLOPS * bench.DD_FMA_INSTRUCTIONS - bench.FP32_NOMINAL_GFLOPS) < 1e-6

@@ -165,6 +165,19 @@ def test_order_inversions_is_the_leg_reordering_sign():
         assert s == (-1.0)**fp.order_inversions(conf)
 
 
+@pytest.mark.parametrize("name", ["3x3_D1_T4_dc16", "4x4_D2_T8_dc2", "3x4_D2_T5_dc3"])
+def test_order_sign_by_count_equals_the_tensor_transpose(name):
+    """The count form of the amplitude's leg-reordering sign (no rank-L1*L2 tensor, so it works on 8x8)
+    equals the graded transpose on every reference sample's leg order."""
+    z, meta, _, _ = _load(name)
+    canon = fp.canonical_names(meta["L1"], meta["L2"], fp.ROW)
+    T = -int(np.asarray(z["confs"][0]).sum())
+    for i, conf in enumerate(z["confs"]):
+        names = meta["ws_names"][i]
+        assert fp.order_sign_by_count(conf, canon, names, T) == fp.order_sign(conf, canon, names, T)
+        assert fp.order_sign_by_count(conf, names, canon, T) == fp.order_sign(conf, names, canon, T)
+
+
 def test_natural_gradient_matches_reference():
     """observer.py:576-675 on the bosonic rows, folded like the gradient, against the reference's
     natural gradient (4x4, cut 2) for a fixed step count and for an error-bounded run."""

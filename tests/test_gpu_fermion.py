@@ -46,8 +46,11 @@ def _blocks_error(host, mk, descs, arrays, dense, a, b):
     return np.abs(mine.transpose(ref.names).storage() - ref.storage()).max(), np.abs(ref.storage()).max()
 
 
-@pytest.mark.parametrize("precision", ["fp64", "dd"])
-@pytest.mark.parametrize("name", CASES)
+# every case in both precisions, except the cut-64 lattice (about a minute per sweep of its chain: float64 only)
+PARAMS = [(n, p) for n in CASES for p in ("fp64", "dd") if not (n.endswith("dc64") and p == "dd")]
+
+
+@pytest.mark.parametrize("name,precision", PARAMS)
 def test_fermionic_chains_match_reference(name, precision):
     from tnsp_gb300.engine import Sampler, estimators, gradient_from
     tol = TOL[precision]
@@ -77,14 +80,15 @@ def test_fermionic_chains_match_reference(name, precision):
         # the signed amplitude of the sampled configurations, in the reference's leg order
         m, x = s.amplitude(conf)
         for b in range(B):
-            sign = fp.order_sign(conf[b], canon, meta["ws_names"][b * ns + k], host.T_charge)
+            sign = fp.order_sign_by_count(conf[b], canon, meta["ws_names"][b * ns + k], host.T_charge)
             got = m[b] * np.exp2(float(x[b])) * sign
             assert abs(got / ws[b, k] - 1.0) < tol["val"], (b, k)
     scalars, delta, edelta = s.read_observer()
     assert scalars[0] == B * ns
     energy, err = estimators(scalars, lat.site_number)
     assert abs(energy - z["energy"][0]) < tol["energy"]
-    assert abs(err - z["energy"][1]) < tol["val"]
+    if B * ns > 1:  # one sample's error bar is the square root of a rounding residual (0 here, 4e-9 there)
+        assert abs(err - z["energy"][1]) < tol["val"]
     grad = lat.unflatten(host.fold_flat(gradient_from(scalars, delta, edelta)))
     errs, scale = [], 0.0
     for a in range(L1):

@@ -106,8 +106,9 @@ def test_precision_names_match_the_header():
     """Python precision names map to the header's TNSP_FP64 / TNSP_FP32 / TNSP_DD values."""
     from tnsp_gb300._lib import PRECISIONS
     header = open(os.path.join(ROOT, "include", "tnsp_gb300.h")).read()
-    values = {k: int(v) for k, v in re.findall(r"#define (TNSP_(?:FP64|FP32|DD)) (\d+)", header)}
-    assert PRECISIONS == {"fp64": values["TNSP_FP64"], "fp32": values["TNSP_FP32"], "dd": values["TNSP_DD"]}
+    values = {k: int(v) for k, v in re.findall(r"#define (TNSP_(?:FP64|FP32|DD|MIXED)) (\d+)", header)}
+    assert PRECISIONS == {"fp64": values["TNSP_FP64"], "fp32": values["TNSP_FP32"], "dd": values["TNSP_DD"],
+                          "mixed": values["TNSP_MIXED"]}
 
 
 def test_sweep_sampling_rejects_unknown_precision_before_the_device():

@@ -12,9 +12,10 @@ LIB_PATH = os.path.join(HERE, "libtnsp_gb300.so")
 TNSP_FP64 = 0
 TNSP_FP32 = 1
 TNSP_DD = 2
+TNSP_MIXED = 3
 TNSP_OPT_JACOBI_SWEEPS = 1
 TNSP_OPT_BLOCKS_PER_SM = 2
-PRECISIONS = {"fp64": TNSP_FP64, "fp32": TNSP_FP32, "dd": TNSP_DD}
+PRECISIONS = {"fp64": TNSP_FP64, "fp32": TNSP_FP32, "dd": TNSP_DD, "mixed": TNSP_MIXED}
 
 _c_int_p = ctypes.POINTER(ctypes.c_int)
 _c_i32_p = ctypes.POINTER(ctypes.c_int32)

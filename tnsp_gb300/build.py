@@ -7,7 +7,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libtnsp_gb300.so")
 SOURCES = [os.path.join(CSRC, f)
-           for f in ("sampler_f64.cu", "sampler_dd.cu", "sampler_f32.cu", "tnsp_capi.cu", "noalloc.cu", "made.cu")]
+           for f in ("sampler_f64.cu", "sampler_dd.cu", "sampler_f32.cu", "sampler_mixed.cu", "tnsp_capi.cu", "noalloc.cu",
+                     "made.cu")]
 DEPS = SOURCES + [os.path.join(CSRC, f) for f in ("sampler_kernels.cuh", "cta_linalg.cuh", "ddfloat.cuh", "launch.h",
                                                   "capi_internal.h")] + [
     os.path.join(os.path.dirname(HERE), "include", "tnsp_gb300.h")
@@ -31,7 +32,7 @@ def up_to_date():
 
 
 def build(force=False, verbose=False):
-    """Compiles libtnsp_gb300.so next to this file unless it is newer than its sources.  The six
+    """Compiles libtnsp_gb300.so next to this file unless it is newer than its sources.  The seven
     translation units compile in parallel, then link into one shared library."""
     if not force and up_to_date():
         return OUT

@@ -67,7 +67,7 @@ struct tnsp_ctx {
   // slots
   int nslots = 0;
   tnsp::Slots slots{};
-  size_t elem = 8;
+  size_t elem = 8;    // bytes of the factorisation type T (shared-memory staging)
   void* d_scratch = nullptr;
   void* d_ones = nullptr;
   int* d_ldims = nullptr;
@@ -99,8 +99,9 @@ const char* tnsp_noalloc_error();
 
 namespace tnsp {
 
-// scratch layout of one slot (elements of the sampler's element type)
-inline void plan_slots(const tnsp_ctx* c, Slots& s) {
+// scratch layout of one slot: byte offsets of its areas, S-typed (storage / contraction type, ssize
+// bytes per element) or T-typed (factorisation type, tsize bytes), each aligned to 256 bytes
+inline void plan_slots(const tnsp_ctx* c, Slots& s, long long tsize, long long ssize) {
   const long long cut = c->cut, D = c->Dmax, Lmax = std::max(c->L1, c->L2);
   const long long chi = cut * D;
   s.capB = cut * D * cut;
@@ -110,30 +111,37 @@ inline void plan_slots(const tnsp_ctx* c, Slots& s) {
   s.capS = D * D * D * cut * cut;
   s.capH = D * D * D * D;
   long long o = 0;
-  auto take = [&](long long n) {
+  auto take = [&](long long n, long long esize) {
     const long long r = o;
-    o += (n + 31) / 32 * 32;
+    o += (n * esize + 255) / 256 * 256;
     return r;
   };
-  s.o_lines[F_UP] = take((long long)c->L1 * c->L2 * s.capB);
-  s.o_lines[F_DOWN] = take((long long)c->L1 * c->L2 * s.capB);
-  s.o_lines[F_LEFT] = take((long long)c->L2 * c->L1 * s.capB);
-  s.o_lines[F_RIGHT] = take((long long)c->L2 * c->L1 * s.capB);
-  s.o_T = take((Lmax + 2) * s.capT);
-  s.o_R = take(s.capR);
-  s.o_tau = take(chi);
-  s.o_X = take(chi * chi);
-  s.o_V = take(chi * chi);
-  s.o_W = take(2 * chi * chi);
-  s.o_sig = take(chi);
-  s.o_E = take((Lmax + 1) * s.capE);
-  s.o_F = take((Lmax + 1) * s.capE);
-  s.o_t1 = take(s.capS);
-  s.o_t2 = take(s.capS);
-  s.o_w0 = take(s.capE);
-  s.o_w1 = take(s.capE);
-  s.o_h = take(s.capH);
+  s.o_lines[F_UP] = take((long long)c->L1 * c->L2 * s.capB, ssize);
+  s.o_lines[F_DOWN] = take((long long)c->L1 * c->L2 * s.capB, ssize);
+  s.o_lines[F_LEFT] = take((long long)c->L2 * c->L1 * s.capB, ssize);
+  s.o_lines[F_RIGHT] = take((long long)c->L2 * c->L1 * s.capB, ssize);
+  s.o_T = take((Lmax + 2) * s.capT, ssize);
+  s.o_G = take(s.capT, tsize);
+  s.o_R = take(s.capR, tsize);
+  s.o_tau = take(chi, tsize);
+  s.o_X = take(chi * chi, tsize);
+  s.o_V = take(chi * chi, tsize);
+  s.o_W = take(2 * chi * chi, tsize);
+  s.o_sig = take(chi, tsize);
+  s.o_E = take((Lmax + 1) * s.capE, ssize);
+  s.o_F = take((Lmax + 1) * s.capE, ssize);
+  s.o_t1 = take(s.capS, ssize);
+  s.o_t2 = take(s.capS, ssize);
+  s.o_w0 = take(s.capE, ssize);
+  s.o_w1 = take(s.capE, ssize);
+  s.o_h = take(s.capH, ssize);
   s.stride = o;
+}
+
+// element sizes of a precision mode: factorisation type T, storage / contraction type S
+inline void precision_sizes(int precision, long long* tsize, long long* ssize) {
+  *tsize = precision == TNSP_FP32 ? 4 : 8;
+  *ssize = (precision == TNSP_FP32 || precision == TNSP_MIXED) ? 4 : 8;
 }
 
 }  // namespace tnsp

@@ -112,7 +112,7 @@ extern "C" int tnsp_amplitude_noalloc(int L1, int L2, int P, const int* dims, co
   shape.cut = cut;
   shape.Dmax = Dmax;
   Slots s{};
-  plan_slots(&shape, s);
+  plan_slots(&shape, s, sizeof(double), sizeof(double));
   const long long chi = (long long)cut * Dmax;
   if (chi > kMaxChi) return err(TNSP_E_TOO_LARGE, "cut * max bond extent exceeds 1024");
   // arena layout: metadata, then one array per kind with an exact per-slot stride (the kernels
@@ -124,7 +124,7 @@ extern "C" int tnsp_amplitude_noalloc(int L1, int L2, int P, const int* dims, co
                       + align256(sizeof(int) * (size_t)ns * 4 * Dmax) // leg charges (zero)
                       + align256(sizeof(int) * (size_t)P)            // physical charges (zero)
                       + align256(sizeof(int) * (size_t)ns);          // site flux (zero)
-  const size_t scratch_slot = align256((size_t)s.stride * sizeof(double));
+  const size_t scratch_slot = align256((size_t)s.stride);
   const size_t ints_slot = sizeof(int) * ((size_t)4 * kMaxL * kMaxL * 3 + 4 * kMaxL + (size_t)cut * (Dmax + 1) +
                                           (size_t)4 * kMaxL * kMaxL * 2 * cut + 4 * kMaxL * kMaxL +
                                           (size_t)kMaxL * 3 * chi + kMaxL + (size_t)(chi * Dmax + chi));
@@ -157,7 +157,7 @@ extern "C" int tnsp_amplitude_noalloc(int L1, int L2, int P, const int* dims, co
   int* d_qleg = (int*)carve(sizeof(int) * (size_t)ns * 4 * Dmax);
   int* d_qphys = (int*)carve(sizeof(int) * (size_t)P);
   int* d_sflux = (int*)carve(sizeof(int) * (size_t)ns);
-  s.stride = (long long)(scratch_slot / sizeof(double));
+  s.stride = (long long)scratch_slot;
   double* d_scratch = (double*)carve(scratch_slot * nslots);
   s.ldims = (int*)carve(sizeof(int) * 4 * kMaxL * kMaxL * 3 * (size_t)nslots);
   s.lexp = (int*)carve(sizeof(int) * 4 * kMaxL * (size_t)nslots);

@@ -5,31 +5,32 @@ namespace tnsp {
 
 void launch_sweep_dd(int grid, size_t smem, cudaStream_t st, const Model& md, const Chains& ch, const Slots& sl,
                      void* scratch, const void* ones, int nsweeps, int observe, int rec_base) {
-  sweep_kernel<dd><<<grid, kThreads, smem, st>>>(md, ch, sl, (dd*)scratch, (const dd*)ones, nsweeps, observe,
-                                              rec_base);
+  sweep_kernel<dd, dd><<<grid, kThreads, smem, st>>>(md, ch, sl, (unsigned char*)scratch, (const dd*)ones, nsweeps,
+                                                     observe, rec_base);
 }
 
 void launch_amplitude_dd(int grid, size_t smem, cudaStream_t st, const Model& md, const Slots& sl, void* scratch,
                          const void* ones, int B, const int32_t* confs, double* out_m, int32_t* out_e,
                          int32_t* status) {
-  amplitude_kernel<dd><<<grid, kThreads, smem, st>>>(md, sl, (dd*)scratch, (const dd*)ones, B, confs, out_m, out_e,
-                                                  status);
+  amplitude_kernel<dd, dd><<<grid, kThreads, smem, st>>>(md, sl, (unsigned char*)scratch, (const dd*)ones, B, confs,
+                                                         out_m, out_e, status);
 }
 
 cudaError_t set_smem_limit_dd(int bytes) {
-  cudaError_t e = cudaFuncSetAttribute(sweep_kernel<dd>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaError_t e = cudaFuncSetAttribute(sweep_kernel<dd, dd>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(sweep_kernel<dd>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    e = cudaFuncSetAttribute(sweep_kernel<dd, dd>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(amplitude_kernel<dd>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    e = cudaFuncSetAttribute(amplitude_kernel<dd, dd>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(amplitude_kernel<dd>, cudaFuncAttributePreferredSharedMemoryCarveout,
+    e = cudaFuncSetAttribute(amplitude_kernel<dd, dd>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              cudaSharedmemCarveoutMaxShared);
   return e;
 }
 
 cudaError_t occupancy_dd(int smem_bytes, int* blocks_per_sm) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sweep_kernel<dd>, kThreads, smem_bytes);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sweep_kernel<dd, dd>, kThreads, smem_bytes);
 }
 
 }  // namespace tnsp

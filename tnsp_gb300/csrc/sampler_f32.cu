@@ -1,35 +1,36 @@
-// float instantiation of the sampler kernels and its host launch wrappers.
+// float32 instantiation of the sampler kernels and its host launch wrappers.
 #include "launch.h"
 
 namespace tnsp {
 
 void launch_sweep_f32(int grid, size_t smem, cudaStream_t st, const Model& md, const Chains& ch, const Slots& sl,
                       void* scratch, const void* ones, int nsweeps, int observe, int rec_base) {
-  sweep_kernel<float><<<grid, kThreads, smem, st>>>(md, ch, sl, (float*)scratch, (const float*)ones, nsweeps, observe,
-                                                  rec_base);
+  sweep_kernel<float, float><<<grid, kThreads, smem, st>>>(md, ch, sl, (unsigned char*)scratch, (const float*)ones,
+                                                           nsweeps, observe, rec_base);
 }
 
 void launch_amplitude_f32(int grid, size_t smem, cudaStream_t st, const Model& md, const Slots& sl, void* scratch,
                           const void* ones, int B, const int32_t* confs, double* out_m, int32_t* out_e,
                           int32_t* status) {
-  amplitude_kernel<float><<<grid, kThreads, smem, st>>>(md, sl, (float*)scratch, (const float*)ones, B, confs, out_m, out_e,
-                                                      status);
+  amplitude_kernel<float, float><<<grid, kThreads, smem, st>>>(md, sl, (unsigned char*)scratch, (const float*)ones, B,
+                                                               confs, out_m, out_e, status);
 }
 
 cudaError_t set_smem_limit_f32(int bytes) {
-  cudaError_t e = cudaFuncSetAttribute(sweep_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaError_t e = cudaFuncSetAttribute(sweep_kernel<float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(sweep_kernel<float>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    e = cudaFuncSetAttribute(sweep_kernel<float, float>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(amplitude_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    e = cudaFuncSetAttribute(amplitude_kernel<float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(amplitude_kernel<float>, cudaFuncAttributePreferredSharedMemoryCarveout,
+    e = cudaFuncSetAttribute(amplitude_kernel<float, float>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              cudaSharedmemCarveoutMaxShared);
   return e;
 }
 
 cudaError_t occupancy_f32(int smem_bytes, int* blocks_per_sm) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sweep_kernel<float>, kThreads, smem_bytes);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sweep_kernel<float, float>, kThreads, smem_bytes);
 }
 
 }  // namespace tnsp

@@ -1,5 +1,11 @@
 // Sweep sampling, local energy and gradient holes of a PEPS on one GPU (kernel templates; the
-// float64 and float32 instantiations live in sampler_f64.cu and sampler_f32.cu).
+// instantiations live in sampler_f64.cu, sampler_dd.cu, sampler_f32.cu and sampler_mixed.cu).
+//
+// Two element types: T, the arithmetic of the factorisations (per-sector QR, pivoted QR and one-sided
+// Jacobi SVD, their staging and factors), and S, the storage and arithmetic of everything else (site
+// tensors, boundary lines, compression tensors, strip environments and their contractions).  The
+// float64, double-float and float32 samplers use one type for both; the mixed sampler keeps the
+// factorisations in double-float and stores and contracts in float32.
 //
 // One thread block owns one Markov chain at a time (persistent blocks stride over thousands of
 // chains).  Inside a block the chain's boundary MPSs, strip environments and compression
@@ -89,10 +95,11 @@ struct Chains {
 };
 
 struct Slots {
-  long long stride;         // elements of T per slot
-  long long o_lines[4];     // line storage per family: [line][site][capB]
-  long long capB, capT, capR, capE, capS, capH;
-  long long o_T, o_R, o_tau, o_X, o_V, o_W, o_sig, o_E, o_F, o_t1, o_t2, o_w0, o_w1, o_h;
+  long long stride;         // bytes per slot
+  long long o_lines[4];     // line storage per family: [line][site][capB] (S); every o_* is a byte offset
+  long long capB, capT, capR, capE, capS, capH;  // capacities in elements
+  // S-typed: o_lines, o_T, o_E, o_F, o_t1, o_t2, o_w0, o_w1, o_h; T-typed: o_G, o_R, o_tau, o_X, o_V, o_W, o_sig
+  long long o_T, o_G, o_R, o_tau, o_X, o_V, o_W, o_sig, o_E, o_F, o_t1, o_t2, o_w0, o_w1, o_h;
   int* ldims;               // [slot][4][kMaxL][kMaxL][3]
   int* lexp;                // [slot][4][kMaxL]
   int* order;               // [slot][cut*(Dmax+1)]: kept singular values, then pivots
@@ -107,6 +114,22 @@ struct Slots {
   int* ilist;               // [slot][chi*Dmax + chi]: packed sector row lists, then column lists
   long long smem_elems;     // dynamic shared memory available to a block, in elements of T
 };
+
+// element conversion between the two types of an engine
+template <class To> struct Cvt {
+  template <class From> static __device__ __forceinline__ To from(From x) { return (To)x; }
+};
+template <> struct Cvt<float> {
+  static __device__ __forceinline__ float from(float x) { return x; }
+  static __device__ __forceinline__ float from(double x) { return (float)x; }
+  static __device__ __forceinline__ float from(dd x) { return x.hi + x.lo; }
+};
+template <> struct Cvt<dd> {
+  static __device__ __forceinline__ dd from(dd x) { return x; }
+  static __device__ __forceinline__ dd from(float x) { return dd(x); }
+  static __device__ __forceinline__ dd from(double x) { return dd(x); }
+};
+template <class To, class From> __device__ __forceinline__ To cvt(From x) { return Cvt<To>::from(x); }
 
 // ------------------------------------------------------------------------------------------
 // random numbers: std::mt19937_64 + libstdc++ 13 distributions (thread 0 only)
@@ -185,11 +208,11 @@ struct Dims3 {
   int a, p, b;
 };
 
-template <class T> struct Chain {
+template <class T, class S> struct Chain {
   const Model& md;
   const Slots& sl;
-  T* slot;
-  const T* A;
+  unsigned char* slot;
+  const S* A;
   int* ldims;
   int* lexp;
   int* order;
@@ -202,6 +225,11 @@ template <class T> struct Chain {
   double* dred;
   double* fl;             // shared [kCounters]: flop counters [0..3], phase cycles [4..]
 
+  // typed view of a byte offset in the slot
+  template <class X> __device__ X* at(long long off) const { return reinterpret_cast<X*>(slot + off); }
+  // block-reduction scratch for S-typed sums (red holds kWarps elements of T, sizeof(S) <= sizeof(T))
+  __device__ S* sred() const { return reinterpret_cast<S*>(red); }
+
   __device__ void count(int k, double f) const {
     if (threadIdx.x == 0) fl[k] += f;
   }
@@ -211,9 +239,9 @@ template <class T> struct Chain {
     if (threadIdx.x == 0) fl[4 + phase] += (double)(clock64() - t0);
   }
 
-  __device__ T* line(int f, int idx, int i) const {
+  __device__ S* line(int f, int idx, int i) const {
     const int ns = (f < 2) ? md.L2 : md.L1;
-    return slot + sl.o_lines[f] + ((long long)idx * ns + i) * sl.capB;
+    return at<S>(sl.o_lines[f]) + ((long long)idx * ns + i) * sl.capB;
   }
   __device__ int* ldim(int f, int idx, int i) const { return ldims + (((f * kMaxL) + idx) * kMaxL + i) * 3; }
 
@@ -430,24 +458,26 @@ template <class T> __device__ T block_dot(const T* x, const T* y, long long n, T
 // ------------------------------------------------------------------------------------------
 // the chain engine
 // ------------------------------------------------------------------------------------------
-template <class T> struct Engine : Chain<T> {
-  using Chain<T>::md;
-  using Chain<T>::sl;
-  using Chain<T>::slot;
-  using Chain<T>::A;
-  using Chain<T>::conf;
-  using Chain<T>::valid;
-  using Chain<T>::eE;
-  using Chain<T>::eF;
-  using Chain<T>::red;
-  using Chain<T>::line;
-  using Chain<T>::ldim;
-  using Chain<T>::site;
-  using Chain<T>::lexp;
-  using Chain<T>::order;
-  using Chain<T>::tic;
-  using Chain<T>::toc;
-  const T* ones;
+template <class T, class S> struct Engine : Chain<T, S> {
+  using Chain<T, S>::md;
+  using Chain<T, S>::sl;
+  using Chain<T, S>::slot;
+  using Chain<T, S>::A;
+  using Chain<T, S>::conf;
+  using Chain<T, S>::valid;
+  using Chain<T, S>::eE;
+  using Chain<T, S>::eF;
+  using Chain<T, S>::red;
+  using Chain<T, S>::line;
+  using Chain<T, S>::ldim;
+  using Chain<T, S>::site;
+  using Chain<T, S>::lexp;
+  using Chain<T, S>::order;
+  using Chain<T, S>::tic;
+  using Chain<T, S>::toc;
+  using Chain<T, S>::sred;
+  template <class X> __device__ X* at(long long off) const { return Chain<T, S>::template at<X>(off); }
+  const S* ones;
   int32_t* status;
   int* lq;
   int* lfl;
@@ -466,7 +496,7 @@ template <class T> struct Engine : Chain<T> {
 
   // line family f at index idx, or the all-ones line beyond the lattice edge
   __device__ bool is_ones(int f, int idx) const { return idx < 0 || idx >= nlines(f); }
-  __device__ const T* lsite(int f, int idx, int i) const { return is_ones(f, idx) ? ones : line(f, idx, i); }
+  __device__ const S* lsite(int f, int idx, int i) const { return is_ones(f, idx) ? ones : line(f, idx, i); }
   __device__ Dims3 lsdim(int f, int idx, int i) const {
     if (is_ones(f, idx)) return Dims3{1, 1, 1};
     const int* d = ldim(f, idx, i);
@@ -474,7 +504,7 @@ template <class T> struct Engine : Chain<T> {
   }
   __device__ int lexpo(int f, int idx) const { return is_ones(f, idx) ? 0 : lexp[f * kMaxL + idx]; }
 
-  __device__ T* Tbuf(int k) const { return slot + sl.o_T + (long long)k * sl.capT; }
+  __device__ S* Tbuf(int k) const { return at<S>(sl.o_T) + (long long)k * sl.capT; }
 
   // charges of line sites and of compression tensors
   __device__ int* lqa(int f, int idx, int i) const {
@@ -589,8 +619,8 @@ template <class T> struct Engine : Chain<T> {
       __syncthreads();
     }
     toc(PH_TWOLINE, t0);
-    T* Rb = slot + sl.o_R;
-    T* tau = slot + sl.o_tau;
+    T* Rb = at<T>(sl.o_R);
+    T* tau = at<T>(sl.o_tau);
     T* sm = smem;
     const long long smcap = sl.smem_elems;
     int* rl = ilist;
@@ -609,9 +639,10 @@ template <class T> struct Engine : Chain<T> {
       int ktot = 0;
       for (int t = 0; t < ns; ++t) ktot += min(s_sec.m[t], s_sec.c[t]);
       const int spare = s_buf[n], spare2 = s_buf[n + 1];
-      T* Tq = Tbuf(spare);  // new T[i] = Q (rows x ktot)
-      T* G = Tbuf(spare2);  // sector staging, later new T[i+1]
-      for (long long t = threadIdx.x; t < (long long)rows * ktot; t += blockDim.x) Tq[t] = (T)0;
+      S* Tq = Tbuf(spare);   // new T[i] = Q (rows x ktot)
+      S* G = Tbuf(spare2);   // new T[i+1] = R T[i+1]
+      T* Gs = at<T>(sl.o_G);  // sector staging when shared memory is too small
+      for (long long t = threadIdx.x; t < (long long)rows * ktot; t += blockDim.x) Tq[t] = (S)0;
       if (threadIdx.x == 0) {
         int o = 0;
         for (int t = 0; t < ns; ++t) {
@@ -626,11 +657,11 @@ template <class T> struct Engine : Chain<T> {
         const int mr = s_sec.m[t], mc = s_sec.c[t], kr = min(mr, mc);
         const int* R_ = rl + s_sec.ro[t];
         const int* C_ = cl + s_sec.co[t];
-        const T* M = Tbuf(s_buf[i]);
-        T* g = ((long long)mr * mc <= smcap) ? sm : G;
+        const S* M = Tbuf(s_buf[i]);
+        T* g = ((long long)mr * mc <= smcap) ? sm : Gs;
         for (long long e = threadIdx.x; e < (long long)mr * mc; e += blockDim.x) {
           const int y = (int)(e / mr), x = (int)(e % mr);
-          g[e] = M[(long long)R_[x] * cols + C_[y]];
+          g[e] = cvt<T>(M[(long long)R_[x] * cols + C_[y]]);
         }
         __syncthreads();
         // power-of-two scaling of the sector to max |g| in [0.5, 1): exact, so Q and R / 2^es are the
@@ -653,7 +684,7 @@ template <class T> struct Engine : Chain<T> {
         block_orgqr_cm(mr, kr, g, tau);
         for (long long e = threadIdx.x; e < (long long)mr * kr; e += blockDim.x) {
           const int y = (int)(e / mr), x = (int)(e % mr);
-          Tq[(long long)R_[x] * ktot + koff + y] = g[e];
+          Tq[(long long)R_[x] * ktot + koff + y] = cvt<S>(g[e]);
         }
         for (int y = threadIdx.x; y < kr; y += blockDim.x) {
           s_kmap[koff + y] = (short)t;
@@ -672,7 +703,7 @@ template <class T> struct Engine : Chain<T> {
       // output tile (4 rows of one sector's R x 4 columns), so one load of T feeds 4 FMAs
       const int dB = s_dd[i + 1] * s_dB[i + 1];
       {
-        const T* Tn = Tbuf(s_buf[i + 1]);
+        const S* Tn = Tbuf(s_buf[i + 1]);
         const int tc = (dB + 3) / 4;
         int kof = 0;
         for (int t = 0; t < ns; ++t) {
@@ -682,19 +713,19 @@ template <class T> struct Engine : Chain<T> {
           const int tr = (kr + 3) / 4;
           for (long long tile = threadIdx.x; tile < (long long)tr * tc; tile += blockDim.x) {
             const int y0 = (int)(tile / tc) * 4, c0 = (int)(tile % tc) * 4;
-            T acc[4][4];
+            S acc[4][4];
 #pragma unroll
             for (int v = 0; v < 4; ++v)
 #pragma unroll
-              for (int u = 0; u < 4; ++u) acc[v][u] = (T)0;
+              for (int u = 0; u < 4; ++u) acc[v][u] = (S)0;
             for (int z = y0; z < mc; ++z) {
-              const T* trow = Tn + (long long)C_[z] * dB + c0;
-              T tv[4];
+              const S* trow = Tn + (long long)C_[z] * dB + c0;
+              S tv[4];
 #pragma unroll
-              for (int u = 0; u < 4; ++u) tv[u] = (c0 + u < dB) ? trow[u] : (T)0;
+              for (int u = 0; u < 4; ++u) tv[u] = (c0 + u < dB) ? trow[u] : (S)0;
 #pragma unroll
               for (int v = 0; v < 4; ++v) {
-                const T rv = (y0 + v < kr) ? rb[(long long)(y0 + v) * mc + z] : (T)0;
+                const S rv = (y0 + v < kr) ? cvt<S>(rb[(long long)(y0 + v) * mc + z]) : (S)0;
 #pragma unroll
                 for (int u = 0; u < 4; ++u) acc[v][u] = fma(rv, tv[u], acc[v][u]);
               }
@@ -737,9 +768,9 @@ template <class T> struct Engine : Chain<T> {
       toc(PH_RABSORB, t0);
     }
     // ---------------- truncating SVD sweep, per sector, global cut ----------------
-    T* X = slot + sl.o_X;
-    T* V = slot + sl.o_V;
-    T* sig = slot + sl.o_sig;
+    T* X = at<T>(sl.o_X);
+    T* V = at<T>(sl.o_V);
+    T* sig = at<T>(sl.o_sig);
     for (int i = n - 1; i >= 1; --i) {
       const int d = s_dd[i], Bc = s_dB[i], rows = s_dA[i], cols = d * Bc, F = s_fl[i];
       const int* qL = tqL(i);
@@ -764,9 +795,9 @@ template <class T> struct Engine : Chain<T> {
         }
       }
       __syncthreads();
-      int S = 0;
-      for (int t = 0; t < ns; ++t) S += min(s_sec.m[t], s_sec.c[t]);
-      const T* M = Tbuf(s_buf[i]);
+      int nsv = 0;
+      for (int t = 0; t < ns; ++t) nsv += min(s_sec.m[t], s_sec.c[t]);
+      const S* M = Tbuf(s_buf[i]);
       // QR-preconditioned one-sided Jacobi (Drmac-Veselic): per sector, A (len x nv, its columns are
       // the block's columns when it is tall, its rows when wide) = Q R P^T by Householder QR with
       // column pivoting, then one-sided Jacobi on the nv columns of R^T (accumulating J), which
@@ -778,8 +809,8 @@ template <class T> struct Engine : Chain<T> {
       __shared__ T* s_xp[kMaxSec];  // A, then Q (len x nv, column-major)
       __shared__ T* s_bp[kMaxSec];  // B = R^T vectors, rotated into W (nv x nv)
       __shared__ T* s_jp[kMaxSec];  // J (nv x nv)
-      T* Wl = slot + sl.o_W;                         // lenvec, packed at s_xo
-      T* Wn = slot + sl.o_W + (long long)chi() * chi();  // nvvec, packed at s_vo
+      T* Wl = at<T>(sl.o_W);                         // lenvec, packed at s_xo
+      T* Wn = at<T>(sl.o_W) + (long long)chi() * chi();  // nvvec, packed at s_vo
       int* perm = order + md.cut;                    // pivots of the current sector (<= chi entries)
       if (threadIdx.x == 0) {
         long long used = 0;
@@ -810,7 +841,7 @@ template <class T> struct Engine : Chain<T> {
         T* x = s_xp[t];
         for (long long e = threadIdx.x; e < (long long)nv * len; e += blockDim.x) {
           const int j = (int)(e / len), q = (int)(e % len);
-          x[e] = caseA ? M[(long long)R_[q] * cols + C_[j]] : M[(long long)R_[j] * cols + C_[q]];
+          x[e] = cvt<T>(caseA ? M[(long long)R_[q] * cols + C_[j]] : M[(long long)R_[j] * cols + C_[q]]);
         }
         const double mm = len, nn = nv;
         this->count(2, 4.0 * mm * mm * nn + 8.0 * mm * nn * nn + 9.0 * nn * nn * nn);
@@ -893,12 +924,12 @@ template <class T> struct Engine : Chain<T> {
         }
         __syncthreads();
       }
-      const int c = md.cut < S ? md.cut : S;
+      const int c = md.cut < nsv ? md.cut : nsv;
       // global selection: descending value, ties to the earlier sector / lower index
-      for (int j = threadIdx.x; j < S; j += blockDim.x) {
+      for (int j = threadIdx.x; j < nsv; j += blockDim.x) {
         const T sj = sig[j];
         int rank = 0;
-        for (int k = 0; k < S; ++k) {
+        for (int k = 0; k < nsv; ++k) {
           const T sk = sig[k];
           rank += (sk > sj) || (sk == sj && k < j);
         }
@@ -914,14 +945,14 @@ template <class T> struct Engine : Chain<T> {
         s_kloc[k] = (short)(j - s_so[t]);
       }
       T smax = 0;
-      for (int j = threadIdx.x; j < S; j += blockDim.x) smax = fmax(smax, sig[j]);
+      for (int j = threadIdx.x; j < nsv; j += blockDim.x) smax = fmax(smax, sig[j]);
       smax = block_max(smax, red);
       int lmaxi = 1;
       for (int t = 0; t < ns; ++t) lmaxi = max(lmaxi, max(s_sec.m[t], s_sec.c[t]));
       const T thr = smax * Eps<T>::value() * (T)lmaxi;
       const int spare = s_buf[n], spare2 = s_buf[n + 1];
-      T* Tn = Tbuf(spare);  // new T[i] (c x cols)
-      for (long long e = threadIdx.x; e < (long long)c * cols; e += blockDim.x) Tn[e] = (T)0;
+      S* Tn = Tbuf(spare);  // new T[i] (c x cols)
+      for (long long e = threadIdx.x; e < (long long)c * cols; e += blockDim.x) Tn[e] = (S)0;
       for (long long e = threadIdx.x; e < (long long)rows * c; e += blockDim.x) Rb[e] = (T)0;
       __syncthreads();
       const int span = max(rows, cols);
@@ -937,7 +968,7 @@ template <class T> struct Engine : Chain<T> {
         // tall block (case A): columns are the nv side; wide block: rows are the nv side
         if (q < mc) {  // right singular vector component at column C[q]
           const T val = caseA ? (sv > thr ? nj[q] / sv : (T)0) : lj[q];
-          Tn[(long long)k * cols + cl[s_sec.co[t] + q]] = val;
+          Tn[(long long)k * cols + cl[s_sec.co[t] + q]] = cvt<S>(val);
         }
         if (q < mr) {  // U*S component at row R[q]
           const T val = caseA ? lj[q] * sv : nj[q];
@@ -952,15 +983,16 @@ template <class T> struct Engine : Chain<T> {
       // new T[i-1] (A d x c) = T[i-1] * US, summing only over the rows of each kept vector's sector
       {
         const int Ad = s_dA[i - 1] * s_dd[i - 1];
-        const T* Tp = Tbuf(s_buf[i - 1]);
-        T* out = Tbuf(spare2);
+        const S* Tp = Tbuf(s_buf[i - 1]);
+        S* out = Tbuf(spare2);
         for (long long e = threadIdx.x; e < (long long)Ad * c; e += blockDim.x) {
           const int xr = (int)(e / c), k = (int)(e % c);
           const int t = s_kmap[k];
           const int* R_ = rl + s_sec.ro[t];
           const int mr = s_sec.m[t];
-          T acc = 0;
-          for (int q = 0; q < mr; ++q) acc = fma(Tp[(long long)xr * rows + R_[q]], Rb[(long long)R_[q] * c + k], acc);
+          S acc = 0;
+          for (int q = 0; q < mr; ++q)
+            acc = fma(Tp[(long long)xr * rows + R_[q]], cvt<S>(Rb[(long long)R_[q] * c + k]), acc);
           out[e] = acc;
         }
         double fl = 0;
@@ -989,12 +1021,12 @@ template <class T> struct Engine : Chain<T> {
       __syncthreads();
       toc(PH_USABSORB, t0);
     }
-    if (n == 1) expo += block_normalize(Tbuf(s_buf[0]), (long long)s_dA[0] * s_dd[0] * s_dB[0], red);
+    if (n == 1) expo += block_normalize(Tbuf(s_buf[0]), (long long)s_dA[0] * s_dd[0] * s_dB[0], sred());
     // store the line with its charges
     for (int i = 0; i < n; ++i) {
       const long long cnt = (long long)s_dA[i] * s_dd[i] * s_dB[i];
-      const T* src = Tbuf(s_buf[i]);
-      T* dst = line(f, idx, i);
+      const S* src = Tbuf(s_buf[i]);
+      S* dst = line(f, idx, i);
       for (long long t = threadIdx.x; t < cnt; t += blockDim.x) dst[t] = src[t];
       int* qa = lqa(f, idx, i);
       int* qb = lqb(f, idx, i);
@@ -1056,8 +1088,8 @@ template <class T> struct Engine : Chain<T> {
   __device__ int fup(int kind) const { return kind == 0 ? F_UP : F_LEFT; }
   __device__ int fdn(int kind) const { return kind == 0 ? F_DOWN : F_RIGHT; }
 
-  __device__ T* Ebuf(int c) const { return slot + sl.o_E + (long long)c * sl.capE; }
-  __device__ T* Fbuf(int c) const { return slot + sl.o_F + (long long)c * sl.capE; }
+  __device__ S* Ebuf(int c) const { return at<S>(sl.o_E) + (long long)c * sl.capE; }
+  __device__ S* Fbuf(int c) const { return at<S>(sl.o_F) + (long long)c * sl.capE; }
   __device__ Dims3 Edims(int kind, int idx, int c) const {
     // E[c] = columns 0..c-1 : (up bond, site bond, down bond) at cut c
     if (c == 0) return Dims3{1, 1, 1};
@@ -1076,31 +1108,31 @@ template <class T> struct Engine : Chain<T> {
   }
 
   // E[c+1] = E[c] x column c (physical index s); writes into dst with exponent returned
-  __device__ int step_left(int kind, int idx, int c, const T* Ein, Dims3 e, int s, T* dst, int mp = 0) {
+  __device__ int step_left(int kind, int idx, int c, const S* Ein, Dims3 e, int s, S* dst, int mp = 0) {
     const long long t0 = tic();
     int l1, l2;
     strip_site_rc(kind, idx, c, l1, l2);
     const SiteView w = site(l1, l2, s, kind == 0 ? 0 : 2, mp);
     strip_left(Ein, e.a, e.p, e.b, lsite(fup(kind), idx - 1, c), lsdim(fup(kind), idx - 1, c), A, w,
-               lsite(fdn(kind), idx + 1, c), lsdim(fdn(kind), idx + 1, c), slot + sl.o_t1, slot + sl.o_t2, dst);
+               lsite(fdn(kind), idx + 1, c), lsdim(fdn(kind), idx + 1, c), at<S>(sl.o_t1), at<S>(sl.o_t2), dst);
     const Dims3 up = lsdim(fup(kind), idx - 1, c), dn = lsdim(fdn(kind), idx + 1, c);
     this->count(3, 2.0 * ((double)e.a * e.p * e.b * up.p * up.b + (double)e.b * up.b * dn.p * w.dr * e.p * up.p +
                           (double)up.b * w.dr * dn.b * e.b * dn.p));
-    const int ex = block_normalize(dst, (long long)up.b * w.dr * dn.b, red);
+    const int ex = block_normalize(dst, (long long)up.b * w.dr * dn.b, sred());
     toc(PH_STRIP, t0);
     return ex;
   }
-  __device__ int step_right(int kind, int idx, int c, const T* Fin, Dims3 f, int s, T* dst, int mp = 0) {
+  __device__ int step_right(int kind, int idx, int c, const S* Fin, Dims3 f, int s, S* dst, int mp = 0) {
     const long long t0 = tic();
     int l1, l2;
     strip_site_rc(kind, idx, c, l1, l2);
     const SiteView w = site(l1, l2, s, kind == 0 ? 0 : 2, mp);
     strip_right(Fin, f.a, f.p, f.b, lsite(fup(kind), idx - 1, c), lsdim(fup(kind), idx - 1, c), A, w,
-                lsite(fdn(kind), idx + 1, c), lsdim(fdn(kind), idx + 1, c), slot + sl.o_t1, slot + sl.o_t2, dst);
+                lsite(fdn(kind), idx + 1, c), lsdim(fdn(kind), idx + 1, c), at<S>(sl.o_t1), at<S>(sl.o_t2), dst);
     const Dims3 up = lsdim(fup(kind), idx - 1, c), dn = lsdim(fdn(kind), idx + 1, c);
     this->count(3, 2.0 * ((double)up.a * up.p * f.a * f.p * f.b + (double)up.a * w.dl * dn.p * f.b * up.p * f.p +
                           (double)up.a * w.dl * dn.a * dn.p * f.b));
-    const int ex = block_normalize(dst, (long long)up.a * w.dl * dn.a, red);
+    const int ex = block_normalize(dst, (long long)up.a * w.dl * dn.a, sred());
     toc(PH_STRIP, t0);
     return ex;
   }
@@ -1121,10 +1153,10 @@ template <class T> struct Engine : Chain<T> {
     ensure(fup(kind), idx - 1);
     ensure(fdn(kind), idx + 1);
     const int n = strip_len(kind);
-    T* F = Fbuf(n);
-    if (threadIdx.x == 0) F[0] = (T)1;
-    T* E = Ebuf(0);
-    if (threadIdx.x == 0) E[0] = (T)1;
+    S* F = Fbuf(n);
+    if (threadIdx.x == 0) F[0] = (S)1;
+    S* E = Ebuf(0);
+    if (threadIdx.x == 0) E[0] = (S)1;
     if (threadIdx.x == 0) {
       eF[n] = 0;
       eE[0] = 0;
@@ -1161,13 +1193,13 @@ template <class T> struct Engine : Chain<T> {
 
   // amplitude with columns c, c+1 of the strip set to s0, s1 (E[c] and F[c+2] valid)
   __device__ void strip_replace2(int kind, int idx, int c, int s0, int s1, double& m, int& ex) {
-    T* w0 = slot + sl.o_w0;
-    T* w1 = slot + sl.o_w1;
+    S* w0 = at<S>(sl.o_w0);
+    S* w1 = at<S>(sl.o_w1);
     const int mp0 = strip_prefix(kind, idx, c);  // the pair's second site counts the first one's new value
     const int e0 = step_left(kind, idx, c, Ebuf(c), Edims(kind, idx, c), s0, w0, mp0);
     const int e1 = step_left(kind, idx, c + 1, w0, Edims(kind, idx, c + 1), s1, w1, mp0 + s0);
     const Dims3 fd = Fdims(kind, idx, c + 2);
-    const T v = block_dot(w1, Fbuf(c + 2), (long long)fd.a * fd.p * fd.b, red);
+    const S v = block_dot(w1, Fbuf(c + 2), (long long)fd.a * fd.p * fd.b, sred());
     m = (double)v;
     ex = eE[c] + e0 + e1 + eF[c + 2] + lexpo(fup(kind), idx - 1) + lexpo(fdn(kind), idx + 1);
   }
@@ -1176,16 +1208,16 @@ template <class T> struct Engine : Chain<T> {
   __device__ void hole0(double& m, int& ex) {
     ensure(F_DOWN, 1);
     const int n = md.L2;
-    T* f0 = slot + sl.o_w0;
-    T* f1 = slot + sl.o_w1;
-    if (threadIdx.x == 0) f0[0] = (T)1;
+    S* f0 = at<S>(sl.o_w0);
+    S* f1 = at<S>(sl.o_w1);
+    if (threadIdx.x == 0) f0[0] = (S)1;
     __syncthreads();
     int e = 0;
     Dims3 fd{1, 1, 1};
     for (int c = n - 1; c >= 0; --c) {
       e += step_right(0, 0, c, f0, fd, conf_at(0, 0, c), f1, strip_prefix(0, 0, c));
       fd = Fdims(0, 0, c);
-      T* t = f0;
+      S* t = f0;
       f0 = f1;
       f1 = t;
     }
@@ -1196,7 +1228,7 @@ template <class T> struct Engine : Chain<T> {
 };
 
 // per-slot integer arrays and the dynamic shared-memory staging area of this block
-template <class T> __device__ void bind_slot(Engine<T>& eng, const Slots& sl, const Model& md) {
+template <class T, class S> __device__ void bind_slot(Engine<T, S>& eng, const Slots& sl, const Model& md) {
   extern __shared__ __align__(16) unsigned char dyn_smem[];
   const long long chi = (long long)md.cut * md.Dmax;
   eng.lq = sl.lq + (long long)blockIdx.x * 4 * kMaxL * kMaxL * 2 * md.cut;
@@ -1259,8 +1291,8 @@ __host__ __device__ inline double fermion_term_sign(const short* conf, int L1, i
 }
 
 // one Metropolis proposal on the term at (kind, idx, c)-(kind, idx, c+1)
-template <class T>
-__device__ void single_term(Engine<T>& eng, const Model& md, int kind, int idx, int c, int t, uint64_t* mt, int* s_mti,
+template <class T, class S>
+__device__ void single_term(Engine<T, S>& eng, const Model& md, int kind, int idx, int c, int t, uint64_t* mt, int* s_mti,
                             double* s_ws_m, int* s_ws_e, int* s_h0_valid, double* s_h0_m, int* s_h0_e, int64_t* accepted) {
   __shared__ int s_sel, s_nn, s_acc, s_skip;
   __shared__ double s_m;
@@ -1346,9 +1378,9 @@ __device__ void single_term(Engine<T>& eng, const Model& md, int kind, int idx, 
   __syncthreads();
 }
 
-template <class T>
-__global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Slots sl, T* scratch, const T* ones,
-                                                         int nsweeps, int observe, int rec_base) {
+template <class T, class S>
+__global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Slots sl, unsigned char* scratch,
+                                                         const S* ones, int nsweeps, int observe, int rec_base) {
   // nsweeps == 0 with observe: observe the current configurations once, without sweeping
   const bool observe_only = nsweeps == 0 && observe;
   const int nsteps = observe_only ? 1 : nsweeps;
@@ -1365,10 +1397,11 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Sl
   if (threadIdx.x < kCounters) s_fl[threadIdx.x] = 0.0;
   __syncthreads();
   const int nsite = md.L1 * md.L2;
-  Engine<T> eng{{md, sl, scratch + (long long)blockIdx.x * sl.stride, (const T*)md.A,
-                 sl.ldims + (long long)blockIdx.x * 4 * kMaxL * kMaxL * 3, sl.lexp + (long long)blockIdx.x * 4 * kMaxL,
-                 sl.order + (long long)blockIdx.x * md.cut * (md.Dmax + 1), s_conf, s_valid, s_eE, s_eF, s_red, s_dred, s_fl},
-                ones, ch.status};
+  Engine<T, S> eng{{md, sl, scratch + (long long)blockIdx.x * sl.stride, (const S*)md.A,
+                    sl.ldims + (long long)blockIdx.x * 4 * kMaxL * kMaxL * 3, sl.lexp + (long long)blockIdx.x * 4 * kMaxL,
+                    sl.order + (long long)blockIdx.x * md.cut * (md.Dmax + 1), s_conf, s_valid, s_eE, s_eF, s_red, s_dred,
+                    s_fl},
+                   ones, ch.status};
   eng.strip_kind = &s_strip_kind;
   eng.strip_idx = &s_strip_idx;
   eng.strip_eupto = &s_strip_eupto;
@@ -1501,9 +1534,9 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Sl
           for (int l2 = 0; l2 < md.L2; ++l2) {
             const Dims3 ed = eng.Edims(0, l1, l2);
             const Dims3 fd = eng.Fdims(0, l1, l2 + 1);
-            T* h = scratch + (long long)blockIdx.x * sl.stride + sl.o_h;
-            T* h1 = scratch + (long long)blockIdx.x * sl.stride + sl.o_t1;
-            T* h2 = scratch + (long long)blockIdx.x * sl.stride + sl.o_t2;
+            S* h = eng.template at<S>(sl.o_h);
+            S* h1 = eng.template at<S>(sl.o_t1);
+            S* h2 = eng.template at<S>(sl.o_t2);
             strip_hole(eng.Ebuf(l2), ed.a, ed.p, ed.b, eng.lsite(F_UP, l1 - 1, l2), eng.lsdim(F_UP, l1 - 1, l2),
                        eng.lsite(F_DOWN, l1 + 1, l2), eng.lsdim(F_DOWN, l1 + 1, l2), eng.Fbuf(l2 + 1), fd.p, h1, h2, h);
             {
@@ -1576,9 +1609,9 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Sl
 }
 
 // amplitude hole(()) of arbitrary configurations (no RNG, no accumulators)
-template <class T>
-__global__ void __launch_bounds__(kThreads) amplitude_kernel(Model md, Slots sl, T* scratch, const T* ones, int B,
-                                                             const int32_t* confs, double* out_m, int32_t* out_e,
+template <class T, class S>
+__global__ void __launch_bounds__(kThreads) amplitude_kernel(Model md, Slots sl, unsigned char* scratch, const S* ones,
+                                                             int B, const int32_t* confs, double* out_m, int32_t* out_e,
                                                              int32_t* status) {
   __shared__ short s_conf[kMaxSites];
   __shared__ unsigned char s_valid[4 * kMaxL];
@@ -1590,10 +1623,11 @@ __global__ void __launch_bounds__(kThreads) amplitude_kernel(Model md, Slots sl,
   if (threadIdx.x < kCounters) s_fl[threadIdx.x] = 0.0;
   __syncthreads();
   const int nsite = md.L1 * md.L2;
-  Engine<T> eng{{md, sl, scratch + (long long)blockIdx.x * sl.stride, (const T*)md.A,
-                 sl.ldims + (long long)blockIdx.x * 4 * kMaxL * kMaxL * 3, sl.lexp + (long long)blockIdx.x * 4 * kMaxL,
-                 sl.order + (long long)blockIdx.x * md.cut * (md.Dmax + 1), s_conf, s_valid, s_eE, s_eF, s_red, s_dred, s_fl},
-                ones, status};
+  Engine<T, S> eng{{md, sl, scratch + (long long)blockIdx.x * sl.stride, (const S*)md.A,
+                    sl.ldims + (long long)blockIdx.x * 4 * kMaxL * kMaxL * 3, sl.lexp + (long long)blockIdx.x * 4 * kMaxL,
+                    sl.order + (long long)blockIdx.x * md.cut * (md.Dmax + 1), s_conf, s_valid, s_eE, s_eF, s_red, s_dred,
+                    s_fl},
+                   ones, status};
   eng.strip_kind = &s_strip_kind;
   eng.strip_idx = &s_strip_idx;
   eng.strip_eupto = &s_strip_eupto;

@@ -1,0 +1,37 @@
+// mixed instantiation of the sampler kernels (double-float factorisations; float32 storage and
+// contractions) and its host launch wrappers.
+#include "launch.h"
+
+namespace tnsp {
+
+void launch_sweep_mx(int grid, size_t smem, cudaStream_t st, const Model& md, const Chains& ch, const Slots& sl,
+                     void* scratch, const void* ones, int nsweeps, int observe, int rec_base) {
+  sweep_kernel<dd, float><<<grid, kThreads, smem, st>>>(md, ch, sl, (unsigned char*)scratch, (const float*)ones,
+                                                        nsweeps, observe, rec_base);
+}
+
+void launch_amplitude_mx(int grid, size_t smem, cudaStream_t st, const Model& md, const Slots& sl, void* scratch,
+                         const void* ones, int B, const int32_t* confs, double* out_m, int32_t* out_e,
+                         int32_t* status) {
+  amplitude_kernel<dd, float><<<grid, kThreads, smem, st>>>(md, sl, (unsigned char*)scratch, (const float*)ones, B,
+                                                            confs, out_m, out_e, status);
+}
+
+cudaError_t set_smem_limit_mx(int bytes) {
+  cudaError_t e = cudaFuncSetAttribute(sweep_kernel<dd, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(sweep_kernel<dd, float>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(amplitude_kernel<dd, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(amplitude_kernel<dd, float>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+  return e;
+}
+
+cudaError_t occupancy_mx(int smem_bytes, int* blocks_per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sweep_kernel<dd, float>, kThreads, smem_bytes);
+}
+
+}  // namespace tnsp

@@ -169,6 +169,7 @@ Model make_model(tnsp_ctx* c) {
   m.Dmax = c->Dmax;
   m.dims = c->d_dims;
   m.off = c->d_off;
+  // site tensors in the storage type: float64, double-float, or float32 (TNSP_FP32 and TNSP_MIXED)
   m.A = c->precision == TNSP_FP64 ? (const void*)c->dA64
         : c->precision == TNSP_DD  ? (const void*)c->dAdd
                                    : (const void*)c->dA32;
@@ -222,8 +223,10 @@ int ensure_slots(tnsp_ctx* ctx) {
   int sms = 0;
   CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
   Slots s{};
-  plan_slots(ctx, s);
-  ctx->elem = ctx->precision == TNSP_FP32 ? 4 : 8;
+  long long tsize = 8, ssize = 8;
+  precision_sizes(ctx->precision, &tsize, &ssize);
+  plan_slots(ctx, s, tsize, ssize);
+  ctx->elem = (size_t)tsize;
   // dynamic shared memory for sector staging.  Per block: 56 KB + ~15 KB static + 1 KB reserved, so
   // three blocks fit in an SM's 228 KB (64 KB allowed only two); the register budget of the sweep
   // kernel (168 per thread) also allows three 128-thread blocks.  With TNSP_OPT_BLOCKS_PER_SM = b the
@@ -240,6 +243,9 @@ int ensure_slots(tnsp_ctx* ctx) {
   } else if (ctx->precision == TNSP_DD) {
     CK(set_smem_limit_dd((int)ctx->smem_bytes));
     CK(occupancy_dd((int)ctx->smem_bytes, &occ));
+  } else if (ctx->precision == TNSP_MIXED) {
+    CK(set_smem_limit_mx((int)ctx->smem_bytes));
+    CK(occupancy_mx((int)ctx->smem_bytes, &occ));
   } else {
     CK(set_smem_limit_f32((int)ctx->smem_bytes));
     CK(occupancy_f32((int)ctx->smem_bytes, &occ));
@@ -249,12 +255,12 @@ int ensure_slots(tnsp_ctx* ctx) {
   if (ctx->blocks_per_sm > 0) occ = ctx->blocks_per_sm;
   // one resident wave of blocks (the occupancy limit per SM), bounded by a scratch budget of 64 GB
   long long want = (long long)std::max(1, occ) * sms;
-  const long long per = s.stride * (long long)ctx->elem + 2LL * ctx->n_params * 8;
+  const long long per = s.stride + 2LL * ctx->n_params * 8;
   const long long budget = 64LL << 30;
   want = std::min(want, std::max(1LL, budget / std::max(1LL, per)));
   want = std::min<long long>(want, std::max(1, ctx->B));
   ctx->nslots = (int)want;
-  CK(cudaMalloc(&ctx->d_scratch, (size_t)s.stride * ctx->elem * ctx->nslots));
+  CK(cudaMalloc(&ctx->d_scratch, (size_t)s.stride * ctx->nslots));
   CK(cudaMalloc(&ctx->d_ones, 16));
   CK(cudaMalloc((void**)&ctx->d_ldims, sizeof(int) * 4 * kMaxL * kMaxL * 3 * ctx->nslots));
   CK(cudaMalloc((void**)&ctx->d_lexp, sizeof(int) * 4 * kMaxL * ctx->nslots));
@@ -279,7 +285,7 @@ int ensure_slots(tnsp_ctx* ctx) {
     fill_ones<double><<<1, 32, 0, ctx->stream>>>((double*)ctx->d_ones);
   else if (ctx->precision == TNSP_DD)
     fill_ones<dd><<<1, 32, 0, ctx->stream>>>((dd*)ctx->d_ones);
-  else
+  else  // float32 storage (TNSP_FP32, TNSP_MIXED)
     fill_ones<float><<<1, 32, 0, ctx->stream>>>((float*)ctx->d_ones);
   CK(cudaGetLastError());
   s.ldims = ctx->d_ldims;
@@ -610,13 +616,13 @@ int tnsp_chains_init(tnsp_ctx* ctx, int B, const int32_t* configs, const uint64_
   if (!ctx) return TNSP_E_ARG;
   if (!ctx->has_lattice || !ctx->has_model) return fail(ctx, TNSP_E_STATE, "upload the lattice and the model first");
   if (B < 1) return fail(ctx, TNSP_E_ARG, "need at least one chain");
-  if (precision != TNSP_FP64 && precision != TNSP_FP32 && precision != TNSP_DD)
+  if (precision != TNSP_FP64 && precision != TNSP_FP32 && precision != TNSP_DD && precision != TNSP_MIXED)
     return fail(ctx, TNSP_E_ARG, "unknown precision");
   if (!configs || !seeds) return fail(ctx, TNSP_E_ARG, "null configs or seeds");
   const int ns = ctx->L1 * ctx->L2;
   for (long long i = 0; i < (long long)B * ns; ++i)
     if (configs[i] < 0 || configs[i] >= ctx->P) return fail(ctx, TNSP_E_ARG, "configuration index out of range");
-  if (precision == TNSP_DD && !ctx->charged) {
+  if ((precision == TNSP_DD || precision == TNSP_MIXED) && !ctx->charged) {
     // block-sparse tensors passed densely without their charges: the structural zeros make
     // rank-deficient boundaries that double-float resolves only to ~1e-3 (float64 is exact there)
     for (int id = 0; id < ns; ++id) {
@@ -754,6 +760,9 @@ int sweep_enqueue(tnsp_ctx* ctx, const SweepPlan& p, int nsweeps, int observe, c
                      0);
   else if (ctx->precision == TNSP_DD)
     launch_sweep_dd(grid, ctx->smem_bytes, st, p.md, p.ch, ctx->slots, ctx->d_scratch, ctx->d_ones, nsweeps, observe,
+                    0);
+  else if (ctx->precision == TNSP_MIXED)
+    launch_sweep_mx(grid, ctx->smem_bytes, st, p.md, p.ch, ctx->slots, ctx->d_scratch, ctx->d_ones, nsweeps, observe,
                     0);
   else
     launch_sweep_f32(grid, ctx->smem_bytes, st, p.md, p.ch, ctx->slots, ctx->d_scratch, ctx->d_ones, nsweeps, observe,
@@ -998,6 +1007,9 @@ int tnsp_amplitude(tnsp_ctx* ctx, int B, const int32_t* configs, double* mantiss
                          dm, de, ctx->d_status);
   else if (ctx->precision == TNSP_DD)
     launch_amplitude_dd(grid, ctx->smem_bytes, ctx->stream, md, ctx->slots, ctx->d_scratch, ctx->d_ones, B, dconf,
+                        dm, de, ctx->d_status);
+  else if (ctx->precision == TNSP_MIXED)
+    launch_amplitude_mx(grid, ctx->smem_bytes, ctx->stream, md, ctx->slots, ctx->d_scratch, ctx->d_ones, B, dconf,
                         dm, de, ctx->d_status);
   else
     launch_amplitude_f32(grid, ctx->smem_bytes, ctx->stream, md, ctx->slots, ctx->d_scratch, ctx->d_ones, B, dconf,

@@ -4,7 +4,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import PRECISIONS, TNSP_DD, TNSP_FP32, TNSP_FP64, ptr
+from ._lib import PRECISIONS, TNSP_DD, TNSP_FP32, TNSP_FP64, TNSP_MIXED, ptr
 
 LN2 = 0.6931471805599453
 
@@ -85,7 +85,7 @@ class Sampler:
         self._check(self.lib.tnsp_set_option(self.ctx, int(option), int(value)), "tnsp_set_option")
 
     def init_chains(self, configs, seeds, discard=0, precision=TNSP_FP64):
-        """``precision``: TNSP_FP64 / TNSP_FP32 / TNSP_DD or one of "fp64", "fp32", "dd"."""
+        """``precision``: TNSP_FP64 / TNSP_FP32 / TNSP_DD / TNSP_MIXED or one of "fp64", "fp32", "dd", "mixed"."""
         if isinstance(precision, str):
             precision = PRECISIONS[precision]
         configs = np.ascontiguousarray(configs, dtype=np.int32)
