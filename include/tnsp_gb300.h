@@ -112,6 +112,26 @@ int tnsp_model_upload(tnsp_ctx* ctx, int n_terms, const int* sites, const int* o
                       int n_entries, const int* out_index, const double* values);
 
 /*
+ * The sweep's proposal tables, laid out as in tnsp_model_upload (no values: only which outputs an input
+ * can hop to, and how many), and per-entry allow flags (NULL: all allowed).  A proposal whose picked
+ * entry is not allowed is rejected before its amplitude ratio and before its uniform draw, as the
+ * reference's restricted subspace rejects it.  n_terms == 0 keeps the energy tables as the proposal
+ * tables and applies `allowed` (one flag per energy-table entry) to them.  A later tnsp_model_upload
+ * drops these tables.
+ * Replaces: SweepSampling's hopping_hamiltonians and restrict_subspace
+ * (tetragono/tetragono/sampling_lattice/sampling.py:81-91, 117-143).
+ */
+int tnsp_model_hopping(tnsp_ctx* ctx, int n_terms, const int* sites, const int* offsets, const int* counts,
+                       int n_entries, const int* out_index, const unsigned char* allowed);
+
+/*
+ * Per-entry allow flags of the energy tables for the observation (NULL: all allowed): an E_loc term whose
+ * entry is not allowed contributes nothing.
+ * Replaces: Observer's restrict_subspace (tetragono/tetragono/sampling_lattice/observer.py:224-233, 364-367).
+ */
+int tnsp_model_energy_restrict(tnsp_ctx* ctx, const unsigned char* allowed);
+
+/*
  * Sets up B independent chains: configs[b*L1*L2 + l1*L2 + l2] are physical indices, seeds[b]
  * seeds chain b's mt19937_64 exactly as TAT.random.seed does, and `discard` uniform_real draws
  * are skipped first (SeedDiffer draws one, tetragono/tetragono/utility.py:146-150).
@@ -131,6 +151,13 @@ int tnsp_chains_init(tnsp_ctx* ctx, int B, const int32_t* configs, const uint64_
 #define TNSP_OPT_BLOCKS_PER_SM 2  /* resident sampler blocks per SM (0 = the most the occupancy
                                      calculator allows, the default); fewer blocks give each chain's
                                      block more shared memory for its factorisations */
+
+/*
+ * Number of chains one launch advances at once (the resident thread blocks, one chain each, planned for
+ * this lattice, cut, precision and TNSP_OPT_BLOCKS_PER_SM): a batch of B chains runs in ceil(B / n)
+ * waves.  Needs tnsp_chains_init.  No reference counterpart (one chain per reference process).
+ */
+int tnsp_resident_chains(tnsp_ctx* ctx, int* n);
 
 /*
  * Sets a context option (TNSP_OPT_*).  Takes effect at the next tnsp_chains_init / tnsp_sweep.  A new

@@ -267,6 +267,65 @@ def run_case(name, kind, L1, L2, D, cut, tensor_seed, chain_seeds, n_therm, n_sa
     print(f"{name}: E/site = {energy:.12f} +- {error:.3e}, saved {os.path.getsize(path)} bytes")
 
 
+def center_fixed(configuration, replacement):
+    """A restricted subspace for the tests: site (1, 1) keeps its value (EdgePoint index)."""
+    return replacement.get((1, 1, 0), configuration[1, 1, 0])[1] == configuration[1, 1, 0][1]
+
+
+def run_restricted_case(name, base, kind, L1, L2, D, cut, tensor_seed, chain_seeds, n_therm, n_samples):
+    """The lattice of case ``base`` sampled with custom hopping Hamiltonians (the spin-flip part of every
+    bond's term, no diagonal proposals) and a restricted subspace (``center_fixed``) in both SweepSampling
+    and Observer (sampling.py:81-91, 117-143; observer.py:224-233, 364-367); saves per chain and sweep the
+    configuration and possibility, per sample ws and E_loc, the energy and the gradient to
+    <name>.npz."""
+    lattice = build_lattice(kind, L1, L2, D, tensor_seed)
+    hopping = {}
+    for positions, H in lattice._hamiltonians.items():
+        Hf = H.copy()
+        for a in range(2):
+            Hf[{"I0": a, "I1": a, "O0": a, "O1": a}] = 0
+            Hf[{"I0": a, "I1": 1 - a, "O0": a, "O1": 1 - a}] = 0
+        hopping[positions] = Hf
+    neel = np.zeros((L1, L2, 1), dtype=np.int64)
+    for l1 in range(L1):
+        for l2 in range(L2):
+            neel[l1, l2, 0] = (l1 + l2) % 2
+    observer = tet.Observer(lattice, enable_energy=True, enable_gradient=True, restrict_subspace=center_fixed)
+    confs, poss, ws_list, eloc_list = [], [], [], []
+    with observer:
+        for seed in chain_seeds:
+            TAT.random.seed(seed)
+            sampling = tet.SweepSampling(lattice, cut, center_fixed, hopping)
+            sampling.configuration.import_configuration(neel)
+            c_confs, c_poss, c_ws, c_eloc = [], [], [], []
+            for step in range(n_therm + n_samples):
+                possibility, configuration = sampling()
+                c_confs.append(configuration.export_configuration()[:, :, 0].copy())
+                c_poss.append(possibility)
+                if step >= n_therm:
+                    before = observer._whole_result_reweight["energy"]
+                    observer(possibility, configuration)
+                    ws = float(configuration.hole(()).storage[0])
+                    c_ws.append(ws)
+                    c_eloc.append((observer._whole_result_reweight["energy"] - before) / (ws * ws / possibility))
+            confs.append(c_confs)
+            poss.append(c_poss)
+            ws_list.append(c_ws)
+            eloc_list.append(c_eloc)
+    out = {"confs": np.array(confs, dtype=np.int64), "possibility": np.array(poss), "ws": np.array(ws_list),
+           "eloc": np.array(eloc_list), "energy": np.array(observer.energy)}
+    grad = observer.gradient
+    for l1 in range(L1):
+        for l2 in range(L2):
+            out[f"grad_{l1}_{l2}"] = dense_site(grad[l1][l2])
+    meta = {"name": name, "base": base, "cut": cut, "chain_seeds": chain_seeds, "n_therm": n_therm,
+            "n_samples": n_samples, "L1": L1, "L2": L2}
+    out["meta"] = np.array(json.dumps(meta))
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: E/site = {observer.energy[0]:.12f}, saved {os.path.getsize(path)} bytes")
+
+
 def run_natural_case(name, kind, L1, L2, D, cut, tensor_seed, chain_seeds, n_therm, n_samples, runs):
     """The chains of case `name` again, observed with enable_natural_gradient; saves the reference's
     natural_gradient_by_conjugate_gradient(step, error) (observer.py:576-675) for every (step, error)
@@ -412,6 +471,9 @@ def _pack_holes(holes, L1, L2):
     return [[dense_site(holes[l1][l2]) for l2 in range(L2)] for l1 in range(L1)]
 
 
+if __name__ == "__main__" and "--restricted" in sys.argv:
+    run_restricted_case("heis_no_3x3_D3_dc4_restricted", "heis_no_3x3_D3_dc4", "no", 3, 3, 3, 4, 1234, [11, 12], 3, 5)
+    sys.exit(0)
 if __name__ == "__main__" and "--workloads" in sys.argv:
     # the benchmark-size lattices: 8x8 Bose U(1) D=6 {-1:2, 0:2, +1:2} with Dcut 36, and 6x6 Bose U(1)
     # D=4 {-1:1, 0:2, +1:1} with Dcut 16 (a few chains and sweeps each: seconds per sample here)

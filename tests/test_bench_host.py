@@ -23,6 +23,15 @@ def test_tau_int_of_short_chains_with_different_means():
     assert tau < 0.7 and info["n_per_chain"] == 25 and info["chains"] == 456
 
 
+def test_tau_int_of_short_chains_with_different_means():
+    """Many short chains whose means differ (as chains still drifting after a short thermalisation):
+    subtracting each chain's own mean keeps the offsets out of the autocorrelation."""
+    rng = np.random.default_rng(2)
+    x = rng.normal(size=(25, 456)) + 3.0 * rng.normal(size=(1, 456))
+    tau, info = bench.tau_int(x)
+    assert tau < 0.7 and info["n_per_chain"] == 25 and info["chains"] == 456
+
+
 def test_tau_int_of_an_ar1_process():
     """x_t = a x_{t-1} + noise has tau_int = (1 + a) / (2 (1 - a)) (= 4.5 for a = 0.8)."""
     rng = np.random.default_rng(1)
@@ -57,6 +66,31 @@ def test_reduce_over_ranks_without_a_group_is_identity():
 def test_workloads_are_consistent():
     for name, w in bench.WORKLOADS.items():
         assert w["precision"] in ("fp64", "dd", "fp32", "mixed"), name
-        assert w["chains"] >= 1 and w["steps"] >= 1
+        assert w["chains"] >= 0 and w["steps"] >= 1  # chains 0: one resident wave
     assert bench.DEFAULT_WORKLOAD in bench.WORKLOADS
     assert abs(bench.DD_NOMINAL_GFLOPS * bench.DD_FMA_INSTRUCTIONS - bench.FP32_NOMINAL_GFLOPS) < 1e-6
+
+
+def test_roofline_fields_follow_from_the_counts():
+    """achieved = algorithmic GEMM flops per sample x samples per launch / launch time; frac = achieved /
+    the measured sustained bf16 rate; the per-sample split comes from the kernel's counters."""
+    from tnsp_gb300._lib import TNSP_DD
+    counters = np.zeros(16)
+    counters[:4] = [4e12, 1e12, 2e12, 0.5e12]   # two steps: contraction, QR, SVD, strip flops
+    counters[4:] = np.arange(1.0, 13.0)
+    r = bench._roofline("heis8x8u1", TNSP_DD, counters, 2, 9000.0, 456)
+    expect = bench.GEMM_FLOPS_PER_SAMPLE["heis8x8u1"] * 456 / 9.0 / 1e12
+    assert abs(r["achieved"] - expect) < 1e-12 * expect
+    peak = bench._measured_peaks().get("bf16_tflops_sustained")
+    if peak:
+        assert abs(r["frac"] - expect / peak) < 1e-12
+    assert abs(r["per_sample"]["qr_svd_algorithmic"] - 1.5e12 / 456) < 1.0
+    assert abs(r["per_sample"]["contraction_executed"] - 2.25e12 / 456) < 1.0
+    assert r["bound"] == "tensor" and r["unit"] == "TFLOP/s"
+
+
+def test_gemm_counts_name_known_workloads():
+    assert set(bench.GEMM_FLOPS_PER_SAMPLE) <= set(bench.WORKLOADS)
+    for members in bench.BATCH_WORKLOADS.values():
+        assert all(n in bench.WORKLOADS for n, _ in members)
+    assert all(v in bench.WORKLOADS for v in bench.PROPOSAL_WORKLOADS.values())

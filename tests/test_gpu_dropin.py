@@ -75,3 +75,53 @@ def test_natural_gradient_matches_reference(name):
             for l2 in range(g.L2):
                 ref = nat[f"natgrad{k}_{l1}_{l2}"]
                 assert np.abs(grad[l1][l2] - ref).max() <= 1e-8 * scale, (k, l1, l2)
+
+
+def center_fixed(configuration, replacement):
+    """The restricted subspace of the golden case: site (1, 1) keeps its value (EdgePoint index), the
+    same callable the reference ran (tests/golden/make_golden.py)."""
+    return replacement.get((1, 1, 0), configuration[1, 1, 0])[1] == configuration[1, 1, 0][1]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "dd"])
+def test_restricted_subspace_and_hopping_hamiltonians_match_reference(precision):
+    """SweepSampling(state, cut, restrict_subspace, hopping_hamiltonians) and Observer(restrict_subspace=...)
+    as the reference runs them (sampling.py:81-91, 117-143; observer.py:364-367): spin-flip-only hopping
+    tables and a restriction that keeps site (1, 1) fixed; configurations bit-exact after every sweep,
+    possibilities, energy and gradient within the golden tolerances."""
+    import os
+    from golden_cases import GOLDEN
+    from test_gpu_parity import TOL, make_lattice
+    from tnsp_gb300.sampling import Observer, SweepSampling
+    tol = TOL[precision]
+    z = np.load(os.path.join(GOLDEN, "heis_no_3x3_D3_dc4_restricted.npz"))
+    g = Golden("heis_no_3x3_D3_dc4")
+    state = make_lattice(g)
+    hopping = {}
+    for positions, table in state._hamiltonians.items():
+        hopping[positions] = {s: [(o, v) for o, v in outs if tuple(o) != tuple(s)] for s, outs in table.items()}
+        hopping[positions] = {s: outs for s, outs in hopping[positions].items() if outs}
+    seeds = [11, 12]
+    chains = len(seeds)
+    nt, ns = 3, 5
+    sampling = SweepSampling(state, g.cut, center_fixed, hopping, chains=chains, seeds=seeds, precision=precision)
+    sampling.configuration.import_configuration(g.neel()[:, :, None])
+    for k in range(nt * chains):
+        possibility, configuration = sampling()
+        ci = k % chains
+        np.testing.assert_array_equal(configuration.export_configuration()[:, :, 0], z["confs"][ci][k // chains])
+    observer = Observer(state, enable_energy=True, enable_gradient=True, restrict_subspace=center_fixed)
+    with observer:
+        for k in range(ns * chains):
+            possibility, configuration = sampling()
+            observer(possibility, configuration)
+            ci = k % chains
+            np.testing.assert_array_equal(configuration.export_configuration()[:, :, 0], z["confs"][ci][nt + k // chains])
+            assert abs(possibility / z["possibility"][ci][nt + k // chains] - 1) < tol["val"]
+    energy, _ = observer.energy
+    assert abs(energy - z["energy"][0]) < tol["energy"]
+    grad = observer.gradient
+    for l1 in range(g.L1):
+        for l2 in range(g.L2):
+            ref = z[f"grad_{l1}_{l2}"]
+            assert np.abs(grad[l1][l2] - ref).max() <= tol["grad"] * max(1.0, np.abs(ref).max())

@@ -117,5 +117,3 @@ def test_sweep_sampling_rejects_unknown_precision_before_the_device():
     lat = random_heisenberg(2, 2, 2, seed=1)
     with pytest.raises(ValueError):
         SweepSampling(lat, 4, precision="fp16")
-    with pytest.raises(NotImplementedError):
-        SweepSampling(lat, 4, restrict_subspace=lambda c: True)

@@ -49,8 +49,12 @@ SIGNATURES = {
     "tnsp_lattice_fermion": (ctypes.c_int, [_c_void_p, _c_dbl_p, ctypes.c_int]),
     "tnsp_model_upload": (ctypes.c_int,
                           [_c_void_p, ctypes.c_int, _c_int_p, _c_int_p, _c_int_p, ctypes.c_int, _c_int_p, _c_dbl_p]),
+    "tnsp_model_hopping": (ctypes.c_int, [_c_void_p, ctypes.c_int, _c_int_p, _c_int_p, _c_int_p, ctypes.c_int, _c_int_p,
+                                          ctypes.POINTER(ctypes.c_ubyte)]),
+    "tnsp_model_energy_restrict": (ctypes.c_int, [_c_void_p, ctypes.POINTER(ctypes.c_ubyte)]),
     "tnsp_chains_init": (ctypes.c_int, [_c_void_p, ctypes.c_int, _c_i32_p, _c_u64_p, ctypes.c_int, ctypes.c_int]),
     "tnsp_set_option": (ctypes.c_int, [_c_void_p, ctypes.c_int, ctypes.c_int]),
+    "tnsp_resident_chains": (ctypes.c_int, [_c_void_p, _c_int_p]),
     "tnsp_sweep": (ctypes.c_int, [_c_void_p, ctypes.c_int, ctypes.c_int]),
     "tnsp_observer_reset": (ctypes.c_int, [_c_void_p]),
     "tnsp_observer_read": (ctypes.c_int, [_c_void_p, _c_dbl_p, _c_dbl_p, _c_dbl_p]),

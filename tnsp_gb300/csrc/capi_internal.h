@@ -46,6 +46,18 @@ struct tnsp_ctx {
   int* d_tab_cnt = nullptr;
   int* d_tab_out = nullptr;
   double* d_tab_val = nullptr;
+  int n_entries = 0;
+  unsigned char* d_e_allow = nullptr;  // energy-table entries inside the observer's restricted subspace
+  // the sweep's proposal tables (tnsp_model_hopping; the energy tables when absent) and their allow flags
+  bool has_hop = false;
+  int hop_entries = 0;
+  int* d_s_hterm = nullptr;
+  int* d_s_vterm = nullptr;
+  int* d_s_hflip = nullptr;
+  int* d_s_tab_off = nullptr;
+  int* d_s_tab_cnt = nullptr;
+  int* d_s_tab_out = nullptr;
+  unsigned char* d_s_allow = nullptr;
   // chains
   int B = 0, precision = TNSP_FP64;
   int32_t* d_conf = nullptr;

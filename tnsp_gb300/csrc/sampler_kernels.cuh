@@ -72,6 +72,18 @@ struct Model {
   int pT;                   // parity of the T leg's charge
   const long long* poff;
   int jacobi_max;           // sweep limit of the one-sided Jacobi SVD
+  // the sweep's proposal tables (SweepSampling's hopping Hamiltonians; the energy tables above unless
+  // replaced), laid out like hterm .. tab_out; allow flags per table entry (null: every entry allowed):
+  // a proposal or an E_loc term whose entry is not allowed is skipped, as a restricted subspace makes
+  // the reference skip it
+  const int* s_hterm;
+  const int* s_vterm;
+  const int* s_hflip;
+  const int* s_tab_off;
+  const int* s_tab_cnt;
+  const int* s_tab_out;
+  const unsigned char* s_allow;
+  const unsigned char* e_allow;
 };
 
 struct Chains {
@@ -273,22 +285,42 @@ template <class T, class S> struct Chain {
 // ------------------------------------------------------------------------------------------
 // contractions
 // ------------------------------------------------------------------------------------------
-// out[(x*l + y), dd, (z*r + w)] = sum_p line[x, p, z] * W(p, dd, y, w)
+// Every contraction below gives each thread kCB outputs that share one operand load (a run of the
+// fastest output index, or of another free index where that one is short): the kCB multiply-add
+// chains are independent, so a thread keeps kCB operations in flight instead of waiting on each
+// result, and the shared operand is read once per kCB outputs.  Tails are handled by clamped reads
+// and guarded writes; each output's sum runs over its terms in the same order as a one-output loop.
+constexpr int kCB = 4;
+
+// out[(x*l + y), dd, (z*r + w)] = sum_p line[x, p, z] * W(p, dd, y, w); a thread computes kCB values of dd
 template <class T>
 __device__ void two_line(const T* __restrict__ line, Dims3 ld, const T* __restrict__ A, SiteView w, T* __restrict__ out) {
   const int Am = ld.a * w.dl, Bm = ld.b * w.dr;
-  const long long n = (long long)Am * w.dd * Bm;
+  const int ddb = (w.dd + kCB - 1) / kCB;
+  const long long n = (long long)Am * ddb * Bm;
   for (long long t = threadIdx.x; t < n; t += blockDim.x) {
     const int col = (int)(t % Bm);
     const long long rest = t / Bm;
-    const int dd = (int)(rest % w.dd);
-    const int row = (int)(rest / w.dd);
+    const int d0 = (int)(rest % ddb) * kCB;
+    const int row = (int)(rest / ddb);
     const int x = row / w.dl, y = row % w.dl, z = col / w.dr, ww = col % w.dr;
-    T acc = 0;
+    T acc[kCB];
+    const T* wp[kCB];
+#pragma unroll
+    for (int v = 0; v < kCB; ++v) {
+      acc[v] = 0;
+      const int d = d0 + v < w.dd ? d0 + v : w.dd - 1;
+      wp[v] = A + w.base + (long long)d * w.sd + (long long)y * w.sl + (long long)ww * w.sr;
+    }
     const T* lp = line + (long long)x * ld.p * ld.b + z;
-    const T* wp = A + w.base + (long long)dd * w.sd + (long long)y * w.sl + (long long)ww * w.sr;
-    for (int p = 0; p < ld.p; ++p) acc = fma(lp[(long long)p * ld.b], wp[(long long)p * w.su], acc);
-    out[t] = acc;
+    for (int p = 0; p < ld.p; ++p) {
+      const T lv = lp[(long long)p * ld.b];
+#pragma unroll
+      for (int v = 0; v < kCB; ++v) acc[v] = fma(lv, wp[v][(long long)p * w.su], acc[v]);
+    }
+#pragma unroll
+    for (int v = 0; v < kCB; ++v)
+      if (d0 + v < w.dd) out[((long long)row * w.dd + d0 + v) * Bm + col] = acc[v];
   }
   __syncthreads();
 }
@@ -298,49 +330,76 @@ template <class T>
 __device__ void strip_left(const T* E, int X, int Y, int Z, const T* up, Dims3 ud, const T* A, SiteView w,
                            const T* dn, Dims3 dd, T* t1, T* t2, T* out) {
   const int U = ud.p, Aa = ud.b, D = dd.p, Bb = dd.b, R = w.dr;
-  // t1[y, z, u, a] = sum_x E[x, y, z] up[x, u, a]
-  long long n = (long long)Y * Z * U * Aa;
+  const int ab = (Aa + kCB - 1) / kCB, bb = (Bb + kCB - 1) / kCB;
+  // t1[y, z, u, a] = sum_x E[x, y, z] up[x, u, a]   (kCB consecutive a)
+  long long n = (long long)Y * Z * U * ab;
   for (long long t = threadIdx.x; t < n; t += blockDim.x) {
-    const int a = (int)(t % Aa);
-    long long r = t / Aa;
+    const int a0 = (int)(t % ab) * kCB;
+    long long r = t / ab;
     const int u = (int)(r % U);
     r /= U;
     const int z = (int)(r % Z);
     const int y = (int)(r / Z);
-    T acc = 0;
-    for (int x = 0; x < X; ++x) acc = fma(E[((long long)x * Y + y) * Z + z], up[((long long)x * U + u) * Aa + a], acc);
-    t1[t] = acc;
+    T acc[kCB];
+#pragma unroll
+    for (int v = 0; v < kCB; ++v) acc[v] = 0;
+    for (int x = 0; x < X; ++x) {
+      const T e = E[((long long)x * Y + y) * Z + z];
+      const T* uu = up + ((long long)x * U + u) * Aa;
+#pragma unroll
+      for (int v = 0; v < kCB; ++v) acc[v] = fma(e, uu[a0 + v < Aa ? a0 + v : Aa - 1], acc[v]);
+    }
+    T* o = t1 + (((long long)y * Z + z) * U + u) * Aa;
+#pragma unroll
+    for (int v = 0; v < kCB; ++v)
+      if (a0 + v < Aa) o[a0 + v] = acc[v];
   }
   __syncthreads();
-  // t2[z, a, d, r] = sum_{y,u} t1[y, z, u, a] W(u, d, y, r)
-  n = (long long)Z * Aa * D * R;
+  // t2[z, a, d, r] = sum_{y,u} t1[y, z, u, a] W(u, d, y, r)   (kCB consecutive a)
+  n = (long long)Z * ab * D * R;
   for (long long t = threadIdx.x; t < n; t += blockDim.x) {
     const int rr = (int)(t % R);
     long long q = t / R;
     const int d = (int)(q % D);
     q /= D;
-    const int a = (int)(q % Aa);
-    const int z = (int)(q / Aa);
-    T acc = 0;
+    const int a0 = (int)(q % ab) * kCB;
+    const int z = (int)(q / ab);
+    T acc[kCB];
+#pragma unroll
+    for (int v = 0; v < kCB; ++v) acc[v] = 0;
     for (int y = 0; y < Y; ++y)
-      for (int u = 0; u < U; ++u)
-        acc = fma(t1[(((long long)y * Z + z) * U + u) * Aa + a],
-                  A[w.base + (long long)u * w.su + (long long)d * w.sd + (long long)y * w.sl + (long long)rr * w.sr], acc);
-    t2[t] = acc;
+      for (int u = 0; u < U; ++u) {
+        const T wv = A[w.base + (long long)u * w.su + (long long)d * w.sd + (long long)y * w.sl + (long long)rr * w.sr];
+        const T* tt = t1 + (((long long)y * Z + z) * U + u) * Aa;
+#pragma unroll
+        for (int v = 0; v < kCB; ++v) acc[v] = fma(tt[a0 + v < Aa ? a0 + v : Aa - 1], wv, acc[v]);
+      }
+#pragma unroll
+    for (int v = 0; v < kCB; ++v)
+      if (a0 + v < Aa) t2[(((long long)z * Aa + a0 + v) * D + d) * R + rr] = acc[v];
   }
   __syncthreads();
-  // out[a, r, b] = sum_{z,d} t2[z, a, d, r] dn[z, d, b]
-  n = (long long)Aa * R * Bb;
+  // out[a, r, b] = sum_{z,d} t2[z, a, d, r] dn[z, d, b]   (kCB consecutive b)
+  n = (long long)Aa * R * bb;
   for (long long t = threadIdx.x; t < n; t += blockDim.x) {
-    const int b = (int)(t % Bb);
-    long long q = t / Bb;
+    const int b0 = (int)(t % bb) * kCB;
+    long long q = t / bb;
     const int rr = (int)(q % R);
     const int a = (int)(q / R);
-    T acc = 0;
+    T acc[kCB];
+#pragma unroll
+    for (int v = 0; v < kCB; ++v) acc[v] = 0;
     for (int z = 0; z < Z; ++z)
-      for (int d = 0; d < D; ++d)
-        acc = fma(t2[(((long long)z * Aa + a) * D + d) * R + rr], dn[((long long)z * D + d) * Bb + b], acc);
-    out[t] = acc;
+      for (int d = 0; d < D; ++d) {
+        const T tv = t2[(((long long)z * Aa + a) * D + d) * R + rr];
+        const T* dp = dn + ((long long)z * D + d) * Bb;
+#pragma unroll
+        for (int v = 0; v < kCB; ++v) acc[v] = fma(tv, dp[b0 + v < Bb ? b0 + v : Bb - 1], acc[v]);
+      }
+    T* o = out + ((long long)a * R + rr) * Bb;
+#pragma unroll
+    for (int v = 0; v < kCB; ++v)
+      if (b0 + v < Bb) o[b0 + v] = acc[v];
   }
   __syncthreads();
 }
@@ -350,49 +409,80 @@ template <class T>
 __device__ void strip_right(const T* F, int Aa, int R, int Bb, const T* up, Dims3 ud, const T* A, SiteView w,
                             const T* dn, Dims3 dd, T* s1, T* s2, T* out) {
   const int X = ud.a, U = ud.p, Z = dd.a, D = dd.p, L = w.dl;
-  // s1[x, u, r, b] = sum_a up[x, u, a] F[a, r, b]
-  long long n = (long long)X * U * R * Bb;
+  const int bb = (Bb + kCB - 1) / kCB, zb = (Z + kCB - 1) / kCB;
+  // s1[x, u, r, b] = sum_a up[x, u, a] F[a, r, b]   (kCB consecutive b)
+  long long n = (long long)X * U * R * bb;
   for (long long t = threadIdx.x; t < n; t += blockDim.x) {
-    const int b = (int)(t % Bb);
-    long long q = t / Bb;
+    const int b0 = (int)(t % bb) * kCB;
+    long long q = t / bb;
     const int rr = (int)(q % R);
     q /= R;
     const int u = (int)(q % U);
     const int x = (int)(q / U);
-    T acc = 0;
-    for (int a = 0; a < Aa; ++a) acc = fma(up[((long long)x * U + u) * Aa + a], F[((long long)a * R + rr) * Bb + b], acc);
-    s1[t] = acc;
+    T acc[kCB];
+#pragma unroll
+    for (int v = 0; v < kCB; ++v) acc[v] = 0;
+    for (int a = 0; a < Aa; ++a) {
+      const T uv = up[((long long)x * U + u) * Aa + a];
+      const T* fp = F + ((long long)a * R + rr) * Bb;
+#pragma unroll
+      for (int v = 0; v < kCB; ++v) acc[v] = fma(uv, fp[b0 + v < Bb ? b0 + v : Bb - 1], acc[v]);
+    }
+    T* o = s1 + (((long long)x * U + u) * R + rr) * Bb;
+#pragma unroll
+    for (int v = 0; v < kCB; ++v)
+      if (b0 + v < Bb) o[b0 + v] = acc[v];
   }
   __syncthreads();
-  // s2[x, l, d, b] = sum_{u,r} s1[x, u, r, b] W(u, d, l, r)
-  n = (long long)X * L * D * Bb;
+  // s2[x, l, d, b] = sum_{u,r} s1[x, u, r, b] W(u, d, l, r)   (kCB consecutive b)
+  n = (long long)X * L * D * bb;
   for (long long t = threadIdx.x; t < n; t += blockDim.x) {
-    const int b = (int)(t % Bb);
-    long long q = t / Bb;
+    const int b0 = (int)(t % bb) * kCB;
+    long long q = t / bb;
     const int d = (int)(q % D);
     q /= D;
     const int l = (int)(q % L);
     const int x = (int)(q / L);
-    T acc = 0;
+    T acc[kCB];
+#pragma unroll
+    for (int v = 0; v < kCB; ++v) acc[v] = 0;
     for (int u = 0; u < U; ++u)
-      for (int rr = 0; rr < R; ++rr)
-        acc = fma(s1[(((long long)x * U + u) * R + rr) * Bb + b],
-                  A[w.base + (long long)u * w.su + (long long)d * w.sd + (long long)l * w.sl + (long long)rr * w.sr], acc);
-    s2[t] = acc;
+      for (int rr = 0; rr < R; ++rr) {
+        const T wv = A[w.base + (long long)u * w.su + (long long)d * w.sd + (long long)l * w.sl + (long long)rr * w.sr];
+        const T* sp = s1 + (((long long)x * U + u) * R + rr) * Bb;
+#pragma unroll
+        for (int v = 0; v < kCB; ++v) acc[v] = fma(sp[b0 + v < Bb ? b0 + v : Bb - 1], wv, acc[v]);
+      }
+    T* o = s2 + (((long long)x * L + l) * D + d) * Bb;
+#pragma unroll
+    for (int v = 0; v < kCB; ++v)
+      if (b0 + v < Bb) o[b0 + v] = acc[v];
   }
   __syncthreads();
-  // out[x, l, z] = sum_{d,b} s2[x, l, d, b] dn[z, d, b]
-  n = (long long)X * L * Z;
+  // out[x, l, z] = sum_{d,b} s2[x, l, d, b] dn[z, d, b]   (kCB consecutive z)
+  n = (long long)X * L * zb;
   for (long long t = threadIdx.x; t < n; t += blockDim.x) {
-    const int z = (int)(t % Z);
-    long long q = t / Z;
+    const int z0 = (int)(t % zb) * kCB;
+    long long q = t / zb;
     const int l = (int)(q % L);
     const int x = (int)(q / L);
-    T acc = 0;
-    for (int d = 0; d < D; ++d)
-      for (int b = 0; b < Bb; ++b)
-        acc = fma(s2[(((long long)x * L + l) * D + d) * Bb + b], dn[((long long)z * D + d) * Bb + b], acc);
-    out[t] = acc;
+    T acc[kCB];
+    const T* dp[kCB];
+#pragma unroll
+    for (int v = 0; v < kCB; ++v) {
+      acc[v] = 0;
+      dp[v] = dn + (long long)(z0 + v < Z ? z0 + v : Z - 1) * D * Bb;
+    }
+    const T* sp = s2 + ((long long)x * L + l) * D * Bb;
+    for (int e = 0; e < D * Bb; ++e) {
+      const T sv = sp[e];
+#pragma unroll
+      for (int v = 0; v < kCB; ++v) acc[v] = fma(sv, dp[v][e], acc[v]);
+    }
+    T* o = out + ((long long)x * L + l) * Z;
+#pragma unroll
+    for (int v = 0; v < kCB; ++v)
+      if (z0 + v < Z) o[z0 + v] = acc[v];
   }
   __syncthreads();
 }
@@ -402,49 +492,82 @@ template <class T>
 __device__ void strip_hole(const T* E, int X, int L, int Z, const T* up, Dims3 ud, const T* dn, Dims3 dd, const T* F,
                            int R, T* h1, T* h2, T* out) {
   const int U = ud.p, Aa = ud.b, D = dd.p, Bb = dd.b;
-  long long n = (long long)L * Z * U * Aa;
+  const int ab = (Aa + kCB - 1) / kCB, bb = (Bb + kCB - 1) / kCB, rb = (R + kCB - 1) / kCB;
+  // h1[l, z, u, a] = sum_x E[x, l, z] up[x, u, a]   (kCB consecutive a)
+  long long n = (long long)L * Z * U * ab;
   for (long long t = threadIdx.x; t < n; t += blockDim.x) {
-    const int a = (int)(t % Aa);
-    long long q = t / Aa;
+    const int a0 = (int)(t % ab) * kCB;
+    long long q = t / ab;
     const int u = (int)(q % U);
     q /= U;
     const int z = (int)(q % Z);
     const int l = (int)(q / Z);
-    T acc = 0;
-    for (int x = 0; x < X; ++x) acc = fma(E[((long long)x * L + l) * Z + z], up[((long long)x * U + u) * Aa + a], acc);
-    h1[t] = acc;
+    T acc[kCB];
+#pragma unroll
+    for (int v = 0; v < kCB; ++v) acc[v] = 0;
+    for (int x = 0; x < X; ++x) {
+      const T e = E[((long long)x * L + l) * Z + z];
+      const T* uu = up + ((long long)x * U + u) * Aa;
+#pragma unroll
+      for (int v = 0; v < kCB; ++v) acc[v] = fma(e, uu[a0 + v < Aa ? a0 + v : Aa - 1], acc[v]);
+    }
+    T* o = h1 + (((long long)l * Z + z) * U + u) * Aa;
+#pragma unroll
+    for (int v = 0; v < kCB; ++v)
+      if (a0 + v < Aa) o[a0 + v] = acc[v];
   }
   __syncthreads();
-  // h2[l, u, a, d, b] = sum_z h1[l, z, u, a] dn[z, d, b]
-  n = (long long)L * U * Aa * D * Bb;
+  // h2[l, u, a, d, b] = sum_z h1[l, z, u, a] dn[z, d, b]   (kCB consecutive b)
+  n = (long long)L * U * Aa * D * bb;
   for (long long t = threadIdx.x; t < n; t += blockDim.x) {
-    const int b = (int)(t % Bb);
-    long long q = t / Bb;
+    const int b0 = (int)(t % bb) * kCB;
+    long long q = t / bb;
     const int d = (int)(q % D);
     q /= D;
     const int a = (int)(q % Aa);
     q /= Aa;
     const int u = (int)(q % U);
     const int l = (int)(q / U);
-    T acc = 0;
-    for (int z = 0; z < Z; ++z)
-      acc = fma(h1[(((long long)l * Z + z) * U + u) * Aa + a], dn[((long long)z * D + d) * Bb + b], acc);
-    h2[t] = acc;
+    T acc[kCB];
+#pragma unroll
+    for (int v = 0; v < kCB; ++v) acc[v] = 0;
+    for (int z = 0; z < Z; ++z) {
+      const T hv = h1[(((long long)l * Z + z) * U + u) * Aa + a];
+      const T* dp = dn + ((long long)z * D + d) * Bb;
+#pragma unroll
+      for (int v = 0; v < kCB; ++v) acc[v] = fma(hv, dp[b0 + v < Bb ? b0 + v : Bb - 1], acc[v]);
+    }
+    T* o = h2 + ((((long long)l * U + u) * Aa + a) * D + d) * Bb;
+#pragma unroll
+    for (int v = 0; v < kCB; ++v)
+      if (b0 + v < Bb) o[b0 + v] = acc[v];
   }
   __syncthreads();
-  n = (long long)U * D * L * R;
+  // out[u, d, l, r] = sum_{a,b} h2[l, u, a, d, b] F[a, r, b]   (kCB consecutive r)
+  n = (long long)U * D * L * rb;
   for (long long t = threadIdx.x; t < n; t += blockDim.x) {
-    const int rr = (int)(t % R);
-    long long q = t / R;
+    const int r0 = (int)(t % rb) * kCB;
+    long long q = t / rb;
     const int l = (int)(q % L);
     q /= L;
     const int d = (int)(q % D);
     const int u = (int)(q / D);
-    T acc = 0;
-    for (int a = 0; a < Aa; ++a)
-      for (int b = 0; b < Bb; ++b)
-        acc = fma(h2[((((long long)l * U + u) * Aa + a) * D + d) * Bb + b], F[((long long)a * R + rr) * Bb + b], acc);
-    out[t] = acc;
+    T acc[kCB];
+#pragma unroll
+    for (int v = 0; v < kCB; ++v) acc[v] = 0;
+    for (int a = 0; a < Aa; ++a) {
+      const T* hp = h2 + ((((long long)l * U + u) * Aa + a) * D + d) * Bb;
+      const T* fp = F + (long long)a * R * Bb;
+      for (int b = 0; b < Bb; ++b) {
+        const T hv = hp[b];
+#pragma unroll
+        for (int v = 0; v < kCB; ++v) acc[v] = fma(hv, fp[(long long)(r0 + v < R ? r0 + v : R - 1) * Bb + b], acc[v]);
+      }
+    }
+    T* o = out + (((long long)u * D + d) * L + l) * R;
+#pragma unroll
+    for (int v = 0; v < kCB; ++v)
+      if (r0 + v < R) o[r0 + v] = acc[v];
   }
   __syncthreads();
 }
@@ -985,15 +1108,29 @@ template <class T, class S> struct Engine : Chain<T, S> {
         const int Ad = s_dA[i - 1] * s_dd[i - 1];
         const S* Tp = Tbuf(s_buf[i - 1]);
         S* out = Tbuf(spare2);
-        for (long long e = threadIdx.x; e < (long long)Ad * c; e += blockDim.x) {
-          const int xr = (int)(e / c), k = (int)(e % c);
+        // a thread computes kCB consecutive rows xr of one column k (one load of U*S per kCB products)
+        const int xb = (Ad + kCB - 1) / kCB;
+        for (long long e = threadIdx.x; e < (long long)xb * c; e += blockDim.x) {
+          const int x0 = (int)(e / c) * kCB, k = (int)(e % c);
           const int t = s_kmap[k];
           const int* R_ = rl + s_sec.ro[t];
           const int mr = s_sec.m[t];
-          S acc = 0;
-          for (int q = 0; q < mr; ++q)
-            acc = fma(Tp[(long long)xr * rows + R_[q]], cvt<S>(Rb[(long long)R_[q] * c + k]), acc);
-          out[e] = acc;
+          S acc[kCB];
+          const S* tp[kCB];
+#pragma unroll
+          for (int v = 0; v < kCB; ++v) {
+            acc[v] = 0;
+            tp[v] = Tp + (long long)(x0 + v < Ad ? x0 + v : Ad - 1) * rows;
+          }
+          for (int q = 0; q < mr; ++q) {
+            const int rq = R_[q];
+            const S us = cvt<S>(Rb[(long long)rq * c + k]);
+#pragma unroll
+            for (int v = 0; v < kCB; ++v) acc[v] = fma(tp[v][rq], us, acc[v]);
+          }
+#pragma unroll
+          for (int v = 0; v < kCB; ++v)
+            if (x0 + v < Ad) out[(long long)(x0 + v) * c + k] = acc[v];
         }
         double fl = 0;
         for (int k = 0; k < c; ++k) fl += 2.0 * Ad * s_sec.m[s_kmap[k]];
@@ -1301,21 +1438,26 @@ __device__ void single_term(Engine<T, S>& eng, const Model& md, int kind, int id
   int l1a, l2a, l1b, l2b;
   eng.strip_site_rc(kind, idx, c, l1a, l2a);
   eng.strip_site_rc(kind, idx, c + 1, l1b, l2b);
-  const int flip = md.hflip[t];
+  const int flip = md.s_hflip[t];
   const int sa = eng.conf[l1a * md.L2 + l2a], sb = eng.conf[l1b * md.L2 + l2b];
   const int in0 = flip ? sb : sa, in1 = flip ? sa : sb;
   const int key = in0 * P + in1;
-  const int cnt = md.tab_cnt[t * P * P + key];
+  const int cnt = md.s_tab_cnt[t * P * P + key];
   if (cnt <= 0) return;  // not in the element pool, or no hopping
+  __shared__ int s_ok;
   if (threadIdx.x == 0) {
     int mti = *s_mti;
     const int pick = draw_uniform_int(mt, mti, cnt);
     *s_mti = mti;
-    const int out = md.tab_out[md.tab_off[t * P * P + key] + pick];
+    const int entry = md.s_tab_off[t * P * P + key] + pick;
+    const int out = md.s_tab_out[entry];
     s_sel = out;
-    s_nn = md.tab_cnt[t * P * P + out];
+    s_nn = md.s_tab_cnt[t * P * P + out];
+    // a restricted subspace rejects the proposal before its ratio and its uniform draw (sampling.py:133-136)
+    s_ok = md.s_allow ? md.s_allow[entry] : 1;
   }
   __syncthreads();
+  if (!s_ok) return;
   const int out = s_sel;
   const int o0 = out / P, o1 = out % P;
   const int na = flip ? o1 : o0, nb = flip ? o0 : o1;
@@ -1439,11 +1581,11 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Sl
       // horizontal bonds, row-major (sampling.py:159-177)
       for (int l1 = 0; l1 < md.L1 && !observe_only; ++l1) {
         bool any = false;
-        for (int l2 = 0; l2 + 1 < md.L2; ++l2) any |= md.hterm[l1 * md.L2 + l2] >= 0;
+        for (int l2 = 0; l2 + 1 < md.L2; ++l2) any |= md.s_hterm[l1 * md.L2 + l2] >= 0;
         if (!any) continue;
         eng.strip_begin(0, l1);
         for (int l2 = 0; l2 + 1 < md.L2; ++l2) {
-          const int t = md.hterm[l1 * md.L2 + l2];
+          const int t = md.s_hterm[l1 * md.L2 + l2];
           if (t < 0) continue;
           single_term(eng, md, 0, l1, l2, t, mt, &s_mti, &s_ws_m, &s_ws_e, &s_h0_valid, &s_h0_m, &s_h0_e, &s_accepted);
         }
@@ -1451,11 +1593,11 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Sl
       // vertical bonds, column-major (sampling.py:178-186)
       for (int l2 = 0; l2 < md.L2 && !observe_only; ++l2) {
         bool any = false;
-        for (int l1 = 0; l1 + 1 < md.L1; ++l1) any |= md.vterm[l1 * md.L2 + l2] >= 0;
+        for (int l1 = 0; l1 + 1 < md.L1; ++l1) any |= md.s_vterm[l1 * md.L2 + l2] >= 0;
         if (!any) continue;
         eng.strip_begin(1, l2);
         for (int l1 = 0; l1 + 1 < md.L1; ++l1) {
-          const int t = md.vterm[l1 * md.L2 + l2];
+          const int t = md.s_vterm[l1 * md.L2 + l2];
           if (t < 0) continue;
           single_term(eng, md, 1, l2, l1, t, mt, &s_mti, &s_ws_m, &s_ws_e, &s_h0_valid, &s_h0_m, &s_h0_e, &s_accepted);
         }
@@ -1494,8 +1636,10 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(Model md, Chains ch, Sl
             const int cnt = md.tab_cnt[t * md.P * md.P + key];
             double total = 0.0;
             for (int k = 0; k < cnt; ++k) {
-              const int out = md.tab_out[md.tab_off[t * md.P * md.P + key] + k];
-              const double v = md.tab_val[md.tab_off[t * md.P * md.P + key] + k];
+              const int entry = md.tab_off[t * md.P * md.P + key] + k;
+              if (md.e_allow && !md.e_allow[entry]) continue;  // outside the restricted subspace (observer.py:364-367)
+              const int out = md.tab_out[entry];
+              const double v = md.tab_val[entry];
               const int o0 = out / md.P, o1 = out % md.P;
               const int na = flip ? o1 : o0, nb = flip ? o0 : o1;
               if (na == sa && nb == sb) {

@@ -127,6 +127,18 @@ void free_chains(tnsp_ctx* c) {
   c->B = 0;
 }
 
+void free_hopping(tnsp_ctx* c) {
+  dfree(c->d_s_hterm);
+  dfree(c->d_s_vterm);
+  dfree(c->d_s_hflip);
+  dfree(c->d_s_tab_off);
+  dfree(c->d_s_tab_cnt);
+  dfree(c->d_s_tab_out);
+  dfree(c->d_s_allow);
+  c->has_hop = false;
+  c->hop_entries = 0;
+}
+
 void free_model(tnsp_ctx* c) {
   dfree(c->d_term_sites);
   dfree(c->d_hterm);
@@ -136,7 +148,50 @@ void free_model(tnsp_ctx* c) {
   dfree(c->d_tab_cnt);
   dfree(c->d_tab_out);
   dfree(c->d_tab_val);
+  dfree(c->d_e_allow);
+  free_hopping(c);
   c->has_model = false;
+}
+
+// Checks a term table (nearest-neighbour two-site terms in the reference's dictionary order) and maps
+// every bond to its term: hterm / vterm [site] = term on (l1,l2)-(l1,l2+1) / (l1,l2)-(l1+1,l2) or -1;
+// hflip[t] = 1 when positions[0] is the second site.  Returns TNSP_OK or a failure code.
+int plan_terms(tnsp_ctx* ctx, int n_terms, const int* sites, const int* offsets, const int* counts, int n_entries,
+               const int* out_index, std::vector<int>& hterm, std::vector<int>& vterm, std::vector<int>& hflip) {
+  const int L1 = ctx->L1, L2 = ctx->L2, P = ctx->P;
+  hterm.assign(L1 * L2, -1);
+  vterm.assign(L1 * L2, -1);
+  hflip.assign(std::max(1, n_terms), 0);
+  for (int t = 0; t < n_terms; ++t) {
+    const int a1 = sites[t * 4], a2 = sites[t * 4 + 1], b1 = sites[t * 4 + 2], b2 = sites[t * 4 + 3];
+    if (a1 < 0 || a1 >= L1 || b1 < 0 || b1 >= L1 || a2 < 0 || a2 >= L2 || b2 < 0 || b2 >= L2)
+      return fail(ctx, TNSP_E_ARG, "term site out of range");
+    int f1 = a1, f2 = a2, flip = 0;
+    if (b1 < a1 || (b1 == a1 && b2 < a2)) {
+      f1 = b1;
+      f2 = b2;
+      flip = 1;
+    }
+    const int g1 = flip ? a1 : b1, g2 = flip ? a2 : b2;
+    int* slot = nullptr;
+    if (g1 == f1 && g2 == f2 + 1)
+      slot = &hterm[f1 * L2 + f2];
+    else if (g2 == f2 && g1 == f1 + 1)
+      slot = &vterm[f1 * L2 + f2];
+    else
+      return fail(ctx, TNSP_E_ARG, "only nearest-neighbour two-site terms are supported");
+    if (*slot >= 0) return fail(ctx, TNSP_E_ARG, "several terms on one bond");
+    *slot = t;
+    hflip[t] = flip;
+    for (int i = 0; i < P * P; ++i) {
+      const int cnt = counts[t * P * P + i];
+      if (cnt > 0 && (offsets[t * P * P + i] < 0 || offsets[t * P * P + i] + cnt > n_entries))
+        return fail(ctx, TNSP_E_ARG, "table entry range out of bounds");
+    }
+  }
+  for (int e = 0; e < n_entries; ++e)
+    if (out_index[e] < 0 || out_index[e] >= P * P) return fail(ctx, TNSP_E_ARG, "table output index out of range");
+  return TNSP_OK;
 }
 
 void free_fermion(tnsp_ctx* c) {
@@ -196,6 +251,14 @@ Model make_model(tnsp_ctx* c) {
   m.qphys = c->d_qphys;
   m.sflux = c->d_sflux;
   m.jacobi_max = c->jacobi_max;
+  m.s_hterm = c->has_hop ? c->d_s_hterm : c->d_hterm;
+  m.s_vterm = c->has_hop ? c->d_s_vterm : c->d_vterm;
+  m.s_hflip = c->has_hop ? c->d_s_hflip : c->d_hflip;
+  m.s_tab_off = c->has_hop ? c->d_s_tab_off : c->d_tab_off;
+  m.s_tab_cnt = c->has_hop ? c->d_s_tab_cnt : c->d_tab_cnt;
+  m.s_tab_out = c->has_hop ? c->d_s_tab_out : c->d_tab_out;
+  m.s_allow = c->d_s_allow;
+  m.e_allow = c->d_e_allow;
   return m;
 }
 
@@ -253,10 +316,14 @@ int ensure_slots(tnsp_ctx* ctx) {
   if (ctx->blocks_per_sm > 0 && occ < ctx->blocks_per_sm)
     return fail(ctx, TNSP_E_ARG, "TNSP_OPT_BLOCKS_PER_SM exceeds the blocks an SM can hold for this kernel");
   if (ctx->blocks_per_sm > 0) occ = ctx->blocks_per_sm;
-  // one resident wave of blocks (the occupancy limit per SM), bounded by a scratch budget of 64 GB
+  // one resident wave of blocks (the occupancy limit per SM), bounded by a scratch budget: 60 % of the
+  // device memory free at this point (the large lattices' slots hold hundreds of MB each; the rest stays
+  // for the caller and for other contexts)
   long long want = (long long)std::max(1, occ) * sms;
   const long long per = s.stride + 2LL * ctx->n_params * 8;
-  const long long budget = 64LL << 30;
+  size_t free_b = 0, total_b = 0;
+  CK(cudaMemGetInfo(&free_b, &total_b));
+  const long long budget = (long long)(0.6 * (double)free_b);
   want = std::min(want, std::max(1LL, budget / std::max(1LL, per)));
   want = std::min<long long>(want, std::max(1, ctx->B));
   ctx->nslots = (int)want;
@@ -369,6 +436,16 @@ int tnsp_ctx_destroy(tnsp_ctx* ctx) {
 }
 
 const char* tnsp_last_error(tnsp_ctx* ctx) { return ctx ? ctx->err.c_str() : tnsp_noalloc_error(); }
+
+int tnsp_resident_chains(tnsp_ctx* ctx, int* n) {
+  if (!ctx || !n) return TNSP_E_ARG;
+  if (!ctx->B) return fail(ctx, TNSP_E_STATE, "no chains");
+  CK(cudaSetDevice(ctx->device));
+  const int r = ensure_slots(ctx);
+  if (r) return r;
+  *n = ctx->nslots;
+  return TNSP_OK;
+}
 
 int tnsp_set_option(tnsp_ctx* ctx, int option, int value) {
   if (!ctx) return TNSP_E_ARG;
@@ -550,38 +627,13 @@ int tnsp_model_upload(tnsp_ctx* ctx, int n_terms, const int* sites, const int* o
   if (!ctx) return TNSP_E_ARG;
   if (!ctx->has_lattice) return fail(ctx, TNSP_E_STATE, "upload the lattice first");
   if (n_terms < 0 || n_entries < 0) return fail(ctx, TNSP_E_ARG, "negative sizes");
+  if (n_entries > 0 && (!out_index || !values)) return fail(ctx, TNSP_E_ARG, "null table arrays");
+  if (n_terms > 0 && (!sites || !offsets || !counts)) return fail(ctx, TNSP_E_ARG, "null table arrays");
   CK(cudaSetDevice(ctx->device));
   const int L1 = ctx->L1, L2 = ctx->L2, P = ctx->P;
-  std::vector<int> hterm(L1 * L2, -1), vterm(L1 * L2, -1), hflip(std::max(1, n_terms), 0);
-  for (int t = 0; t < n_terms; ++t) {
-    const int a1 = sites[t * 4], a2 = sites[t * 4 + 1], b1 = sites[t * 4 + 2], b2 = sites[t * 4 + 3];
-    if (a1 < 0 || a1 >= L1 || b1 < 0 || b1 >= L1 || a2 < 0 || a2 >= L2 || b2 < 0 || b2 >= L2)
-      return fail(ctx, TNSP_E_ARG, "term site out of range");
-    int f1 = a1, f2 = a2, flip = 0;
-    if (b1 < a1 || (b1 == a1 && b2 < a2)) {
-      f1 = b1;
-      f2 = b2;
-      flip = 1;
-    }
-    const int g1 = flip ? a1 : b1, g2 = flip ? a2 : b2;
-    int* slot = nullptr;
-    if (g1 == f1 && g2 == f2 + 1)
-      slot = &hterm[f1 * L2 + f2];
-    else if (g2 == f2 && g1 == f1 + 1)
-      slot = &vterm[f1 * L2 + f2];
-    else
-      return fail(ctx, TNSP_E_ARG, "only nearest-neighbour two-site terms are supported");
-    if (*slot >= 0) return fail(ctx, TNSP_E_ARG, "several terms on one bond");
-    *slot = t;
-    hflip[t] = flip;
-    for (int i = 0; i < P * P; ++i) {
-      const int cnt = counts[t * P * P + i];
-      if (cnt > 0 && (offsets[t * P * P + i] < 0 || offsets[t * P * P + i] + cnt > n_entries))
-        return fail(ctx, TNSP_E_ARG, "table entry range out of bounds");
-    }
-  }
-  for (int e = 0; e < n_entries; ++e)
-    if (out_index[e] < 0 || out_index[e] >= P * P) return fail(ctx, TNSP_E_ARG, "table output index out of range");
+  std::vector<int> hterm, vterm, hflip;
+  const int r = plan_terms(ctx, n_terms, sites, offsets, counts, n_entries, out_index, hterm, vterm, hflip);
+  if (r) return r;
   const bool terms_changed = !ctx->has_model || n_terms != ctx->n_terms;
   free_model(ctx);
   const size_t tp = (size_t)std::max(1, n_terms) * P * P;
@@ -606,8 +658,62 @@ int tnsp_model_upload(tnsp_ctx* ctx, int n_terms, const int* sites, const int* o
   CK(cudaMemcpy(ctx->d_vterm, vterm.data(), sizeof(int) * L1 * L2, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_hflip, hflip.data(), sizeof(int) * hflip.size(), cudaMemcpyHostToDevice));
   ctx->n_terms = n_terms;
+  ctx->n_entries = n_entries;
   ctx->has_model = true;
   if (terms_changed) free_slots(ctx);  // the contribution buffer depends on n_terms
+  return TNSP_OK;
+}
+
+int tnsp_model_hopping(tnsp_ctx* ctx, int n_terms, const int* sites, const int* offsets, const int* counts,
+                       int n_entries, const int* out_index, const unsigned char* allowed) {
+  if (!ctx) return TNSP_E_ARG;
+  if (!ctx->has_model) return fail(ctx, TNSP_E_STATE, "upload the model first");
+  if (n_terms < 0 || n_entries < 0) return fail(ctx, TNSP_E_ARG, "negative sizes");
+  CK(cudaSetDevice(ctx->device));
+  free_hopping(ctx);
+  const int L1 = ctx->L1, L2 = ctx->L2, P = ctx->P;
+  if (n_terms == 0) {
+    // the energy tables propose; only the allow flags are new
+    if (!allowed) return TNSP_OK;
+    CK(cudaMalloc((void**)&ctx->d_s_allow, std::max(1, ctx->n_entries)));
+    if (ctx->n_entries > 0) CK(cudaMemcpy(ctx->d_s_allow, allowed, ctx->n_entries, cudaMemcpyHostToDevice));
+    ctx->hop_entries = ctx->n_entries;
+    return TNSP_OK;
+  }
+  if (!sites || !offsets || !counts || (n_entries > 0 && !out_index)) return fail(ctx, TNSP_E_ARG, "null table arrays");
+  std::vector<int> hterm, vterm, hflip;
+  const int r = plan_terms(ctx, n_terms, sites, offsets, counts, n_entries, out_index, hterm, vterm, hflip);
+  if (r) return r;
+  const size_t tp = (size_t)n_terms * P * P;
+  CK(cudaMalloc((void**)&ctx->d_s_hterm, sizeof(int) * L1 * L2));
+  CK(cudaMalloc((void**)&ctx->d_s_vterm, sizeof(int) * L1 * L2));
+  CK(cudaMalloc((void**)&ctx->d_s_hflip, sizeof(int) * hflip.size()));
+  CK(cudaMalloc((void**)&ctx->d_s_tab_off, sizeof(int) * tp));
+  CK(cudaMalloc((void**)&ctx->d_s_tab_cnt, sizeof(int) * tp));
+  CK(cudaMalloc((void**)&ctx->d_s_tab_out, sizeof(int) * std::max(1, n_entries)));
+  CK(cudaMemcpy(ctx->d_s_hterm, hterm.data(), sizeof(int) * L1 * L2, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_s_vterm, vterm.data(), sizeof(int) * L1 * L2, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_s_hflip, hflip.data(), sizeof(int) * hflip.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_s_tab_off, offsets, sizeof(int) * tp, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_s_tab_cnt, counts, sizeof(int) * tp, cudaMemcpyHostToDevice));
+  if (n_entries > 0) CK(cudaMemcpy(ctx->d_s_tab_out, out_index, sizeof(int) * n_entries, cudaMemcpyHostToDevice));
+  if (allowed) {
+    CK(cudaMalloc((void**)&ctx->d_s_allow, std::max(1, n_entries)));
+    if (n_entries > 0) CK(cudaMemcpy(ctx->d_s_allow, allowed, n_entries, cudaMemcpyHostToDevice));
+  }
+  ctx->has_hop = true;
+  ctx->hop_entries = n_entries;
+  return TNSP_OK;
+}
+
+int tnsp_model_energy_restrict(tnsp_ctx* ctx, const unsigned char* allowed) {
+  if (!ctx) return TNSP_E_ARG;
+  if (!ctx->has_model) return fail(ctx, TNSP_E_STATE, "upload the model first");
+  CK(cudaSetDevice(ctx->device));
+  dfree(ctx->d_e_allow);
+  if (!allowed) return TNSP_OK;
+  CK(cudaMalloc((void**)&ctx->d_e_allow, std::max(1, ctx->n_entries)));
+  if (ctx->n_entries > 0) CK(cudaMemcpy(ctx->d_e_allow, allowed, ctx->n_entries, cudaMemcpyHostToDevice));
   return TNSP_OK;
 }
 

@@ -84,6 +84,37 @@ class Sampler:
         """A context option (``_lib.TNSP_OPT_JACOBI_SWEEPS`` / ``_lib.TNSP_OPT_BLOCKS_PER_SM``)."""
         self._check(self.lib.tnsp_set_option(self.ctx, int(option), int(value)), "tnsp_set_option")
 
+    def set_hopping(self, tables=None, allowed=None):
+        """The sweep's proposal tables ({positions: element table}, as the lattice's Hamiltonians;
+        None: the energy tables propose) and one 0/1 flag per entry of the proposal tables (None: every
+        entry allowed); see tnsp_model_hopping."""
+        from .lattice import table_arrays
+        flags = None if allowed is None else np.ascontiguousarray(allowed, dtype=np.uint8)
+        fptr = ptr(flags, ctypes.c_ubyte)
+        if tables is None:
+            self._check(self.lib.tnsp_model_hopping(self.ctx, 0, None, None, None, 0, None, fptr), "tnsp_model_hopping")
+            return
+        n, sites, offs, cnts, outs, _ = table_arrays(self.lattice.P, tables)
+        if flags is not None and flags.size != outs.size:
+            raise ValueError("one allow flag per proposal-table entry")
+        self._check(self.lib.tnsp_model_hopping(self.ctx, n, ptr(sites, ctypes.c_int), ptr(offs, ctypes.c_int),
+                                                ptr(cnts, ctypes.c_int), len(outs), ptr(outs, ctypes.c_int), fptr),
+                    "tnsp_model_hopping")
+
+    def restrict_energy(self, allowed=None):
+        """One 0/1 flag per entry of the energy tables: E_loc terms of disallowed entries are skipped (None:
+        all allowed); see tnsp_model_energy_restrict."""
+        flags = None if allowed is None else np.ascontiguousarray(allowed, dtype=np.uint8)
+        self._check(self.lib.tnsp_model_energy_restrict(self.ctx, ptr(flags, ctypes.c_ubyte)),
+                    "tnsp_model_energy_restrict")
+        self.energy_restricted = flags is not None
+
+    def resident_chains(self):
+        """Chains one launch advances at once (one resident thread block each)."""
+        n = ctypes.c_int()
+        self._check(self.lib.tnsp_resident_chains(self.ctx, ctypes.byref(n)), "tnsp_resident_chains")
+        return n.value
+
     def init_chains(self, configs, seeds, discard=0, precision=TNSP_FP64):
         """``precision``: TNSP_FP64 / TNSP_FP32 / TNSP_DD / TNSP_MIXED or one of "fp64", "fp32", "dd", "mixed"."""
         if isinstance(precision, str):

@@ -252,30 +252,36 @@ class SamplingLattice:
 
     def term_arrays(self):
         """Flattened Hamiltonian tables in the layout of tnsp_model_upload."""
-        P = self.P
-        terms = list(self._hamiltonians.items())
-        sites, offsets, counts, outs, vals = [], [], [], [], []
-        for positions, table in terms:
-            if len(positions) != 2:
-                raise NotImplementedError("only two-site terms are supported")
-            (a1, a2, ao), (b1, b2, bo) = positions
-            if ao != 0 or bo != 0:
-                raise NotImplementedError("only orbit 0 is supported")
-            sites += [a1, a2, b1, b2]
-            for s0 in range(P):
-                for s1 in range(P):
-                    entries = table.get((s0, s1))
-                    if entries is None:
-                        offsets.append(0)
-                        counts.append(-1)
-                        continue
-                    offsets.append(len(outs))
-                    counts.append(len(entries))
-                    for (o0, o1), v in entries:
-                        outs.append(o0 * P + o1)
-                        vals.append(v)
-        return (len(terms), np.array(sites, dtype=np.int32), np.array(offsets, dtype=np.int32),
-                np.array(counts, dtype=np.int32), np.array(outs, dtype=np.int32), np.array(vals, dtype=np.float64))
+        return table_arrays(self.P, self._hamiltonians)
+
+
+def table_arrays(P, tables):
+    """Flattened element tables {positions: {input tuple: [(output tuple, value), ...]}} in the layout
+    of tnsp_model_upload / tnsp_model_hopping: (n_terms, sites, offsets, counts, out_index, values); the
+    entries follow the dictionary order of the terms, inputs row-major, outputs in table order."""
+    terms = list(tables.items())
+    sites, offsets, counts, outs, vals = [], [], [], [], []
+    for positions, table in terms:
+        if len(positions) != 2:
+            raise NotImplementedError("only two-site terms are supported")
+        (a1, a2, ao), (b1, b2, bo) = positions
+        if ao != 0 or bo != 0:
+            raise NotImplementedError("only orbit 0 is supported")
+        sites += [a1, a2, b1, b2]
+        for s0 in range(P):
+            for s1 in range(P):
+                entries = table.get((s0, s1))
+                if entries is None:
+                    offsets.append(0)
+                    counts.append(-1)
+                    continue
+                offsets.append(len(outs))
+                counts.append(len(entries))
+                for (o0, o1), v in entries:
+                    outs.append(o0 * P + o1)
+                    vals.append(v)
+    return (len(terms), np.array(sites, dtype=np.int32), np.array(offsets, dtype=np.int32),
+            np.array(counts, dtype=np.int32), np.array(outs, dtype=np.int32), np.array(vals, dtype=np.float64))
 
 
 # --------------------------------------------------------------------------------------------

@@ -17,9 +17,10 @@ chains' samples without device work.  ``Observer.__call__`` therefore only check
 accumulation already happened on the device, and ``energy`` / ``gradient`` read the reduced
 accumulators.
 
-Only the features of the sweep / E_loc / gradient / natural-gradient (conjugate gradient) path are
-mirrored: no restricted subspace other than charge conservation, no custom hopping Hamiltonians, no
-extra observer sets, no cached deltas or configurations, no pseudo-inverse natural gradient
+Only the features of the sweep / E_loc / gradient / natural-gradient path are mirrored.  Restricted
+subspaces and custom hopping Hamiltonians are accepted when the restriction depends on the replaced
+sites only (as tetraku's ``restrict_Sz`` does): it is evaluated here for every table entry and the
+device skips the disallowed ones.  No cached deltas or configurations, no off-diagonal observer sets
 (``NotImplementedError`` where the reference would accept them).
 """
 import numpy as np
@@ -59,6 +60,54 @@ def allreduce_sum(arrays):
         out.append(flat[o:o + a.size].reshape(a.shape))
         o += a.size
     return out
+
+
+def _edge_point(charges, p):
+    """The reference's EdgePoint (symmetry, index within its segment) of physical index p, from the
+    per-index charges of the physical edge (one segment per charge, in edge order)."""
+    q = charges[p]
+    return (q, p - charges.index(q))
+
+
+class _RestrictionView:
+    """What a restriction callable reads: ``configuration[l1, l2, orbit]`` as an EdgePoint and
+    ``configuration.owner``."""
+
+    def __init__(self, owner, conf, charges):
+        self.owner = owner
+        self._conf = conf
+        self._charges = charges
+
+    def __getitem__(self, key):
+        l1, l2, _ = key
+        return _edge_point(self._charges, int(self._conf[l1, l2]))
+
+
+def restriction_flags(owner, tables, restrict, conf):
+    """One 0/1 flag per entry of ``tables`` (layout of ``lattice.table_arrays``): whether
+    ``restrict(configuration, replacement)`` allows replacing the term's sites, from the entry's input
+    values, by its output values (sampling.py:133-136, observer.py:364-367).  It is evaluated on two
+    backgrounds (``conf`` and its complement at the other sites); a restriction whose answer depends on
+    sites outside the replaced ones raises NotImplementedError (the device cannot call it per proposal)."""
+    charges = list(owner.charges[1]) if owner.charges is not None else [0] * owner.P
+    conf = np.array(conf, dtype=np.int64).reshape(owner.L1, owner.L2)
+    backgrounds = [conf, (owner.P - 1) - conf]
+    flags = []
+    for positions, table in tables.items():
+        for s0 in range(owner.P):
+            for s1 in range(owner.P):
+                for s_out, _ in table.get((s0, s1), []):
+                    replacement = {tuple(p): _edge_point(charges, int(v)) for p, v in zip(positions, s_out)}
+                    answers = set()
+                    for bg in backgrounds:
+                        c = bg.copy()
+                        for p, v in zip(positions, (s0, s1)):
+                            c[p[0], p[1]] = v
+                        answers.add(bool(restrict(_RestrictionView(owner, c, charges), replacement)))
+                    if len(answers) != 1:
+                        raise NotImplementedError("restrict_subspace depends on sites outside the replaced ones")
+                    flags.append(1 if answers.pop() else 0)
+    return np.array(flags, dtype=np.uint8)
 
 
 def default_seeds(chains, seed_base=0):
@@ -116,10 +165,8 @@ class SweepSampling:
 
     def __init__(self, owner, cut_dimension, restrict_subspace=None, hopping_hamiltonians=None, *, chains=1,
                  seeds=None, seed_base=0, discard=0, precision="fp64", device=0):
-        if restrict_subspace is not None:
-            raise NotImplementedError("restrict_subspace: only charge conservation of the model is supported")
-        if hopping_hamiltonians is not None:
-            raise NotImplementedError("custom hopping Hamiltonians are not supported")
+        self._restrict = restrict_subspace
+        self._hopping = hopping_hamiltonians
         self.owner = owner
         self._cut_dimension = cut_dimension
         self.chains = chains
@@ -137,8 +184,15 @@ class SweepSampling:
         self.configuration = _PendingImport(self)
 
     def _set_start(self, config):
+        if self._restrict is not None or self._hopping is not None:
+            tables = self._hopping if self._hopping is not None else self.owner._hamiltonians
+            allowed = None
+            if self._restrict is not None:
+                allowed = restriction_flags(self.owner, tables, self._restrict, config)
+            self._engine.set_hopping(self._hopping, allowed)
         self._engine.init_chains(np.asarray(config, dtype=np.int32), self.seeds, discard=self.discard,
                                  precision=self.precision)
+        self._start_config = np.array(config)
         self._started = True
 
     def refresh_all(self):
@@ -152,7 +206,7 @@ class SweepSampling:
             observer = getattr(self.owner, "_active_observer", None)
             observing = observer is not None
             if observing and observer._engine is not self._engine:
-                observer._bind(self._engine)
+                observer._bind(self._engine, self._start_config)
             if self._engine._uploaded_version != self.owner.version:
                 self._engine.upload()
             self._engine.sweep(1, observe=observing)
@@ -178,10 +232,11 @@ class Observer:
     def __init__(self, owner, *, observer_set=None, enable_energy=False, enable_gradient=False,
                  enable_natural_gradient=False, cache_natural_delta=None, cache_configuration=False,
                  restrict_subspace=None, classical_energy=None):
-        if cache_natural_delta or cache_configuration or restrict_subspace is not None or classical_energy is not None:
+        if cache_natural_delta or cache_configuration or classical_energy is not None:
             raise NotImplementedError("only energy, gradient, natural-gradient and diagonal observer-set observation "
                                       "are supported")
         self.owner = owner
+        self._restrict = restrict_subspace
         # observer_set: {name: {positions: element table}}, tables as the lattice's Hamiltonian tables
         # ({input tuple: [(output tuple, value)]}); diagonal operators only (their value needs the sampled
         # configuration alone, as Sz or n at any distance)
@@ -244,10 +299,19 @@ class Observer:
                     total += x
                 whole += (total * w, total * w * w, total * total * w * w)
 
-    def _bind(self, engine):
+    def restrict_subspace(self, restrict_subspace):
+        """``Observer.restrict_subspace`` (observer.py:224-233): E_loc terms that leave the subspace are
+        skipped."""
+        self._restrict = restrict_subspace
+
+    def _bind(self, engine, start=None):
         if self._engine is not None:
             raise RuntimeError("one observer context observes one SweepSampling")
         self._engine = engine
+        if self._restrict is not None:
+            engine.restrict_energy(restriction_flags(self.owner, self.owner._hamiltonians, self._restrict, start))
+        elif getattr(engine, "energy_restricted", False):
+            engine.restrict_energy(None)  # an earlier observer's restriction does not carry over
         engine.keep_holes(self._enable_natural)
         engine.reset_observer()
 
