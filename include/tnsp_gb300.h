@@ -227,6 +227,15 @@ int tnsp_holes_keep(tnsp_ctx* ctx, int enable);
 int tnsp_holes_count(tnsp_ctx* ctx, int64_t* rows);
 int tnsp_holes_gemv(tnsp_ctx* ctx, int transpose, const double* x, double* y);
 
+/*
+ * gram (rows x rows, row-major, rows = tnsp_holes_count) = H H^T over the kept hole rows, float64, one
+ * launch: the sample-space matrix of the pseudo-inverse natural gradient, whose T = D D^T follows on the
+ * host from it, H delta and delta.delta (D = the rows minus their weighted mean delta).
+ * Replaces: the D D^T product of natural_gradient_by_direct_pseudo_inverse
+ * (tetragono/tetragono/sampling_lattice/observer.py:697-907, single-process form :902-907).
+ */
+int tnsp_holes_gram(tnsp_ctx* ctx, double* gram);
+
 /* Copies the chains' current configurations (export_configuration, lattice.py:208-229) and, if
  * not NULL, the sampling weight log|ws|^2 of their last sweep (log of `possibility`). */
 int tnsp_chains_read(tnsp_ctx* ctx, int32_t* configs, double* log_possibility);

@@ -125,3 +125,40 @@ def test_restricted_subspace_and_hopping_hamiltonians_match_reference(precision)
         for l2 in range(g.L2):
             ref = z[f"grad_{l1}_{l2}"]
             assert np.abs(grad[l1][l2] - ref).max() <= tol["grad"] * max(1.0, np.abs(ref).max())
+
+
+def test_hole_row_gram_product_and_pseudo_inverse():
+    """tnsp_holes_gram (H H^T over the device-kept hole rows, one launch) equals the products built from
+    tnsp_holes_gemv, and the pseudo-inverse natural gradient built on it equals the single-process equation
+    (observer.py:902-907) evaluated from the rows read back."""
+    from test_gpu_parity import make_lattice
+    from tnsp_gb300.sampling import Observer, SweepSampling
+    g = Golden("heis_u1_4x4_D111_dc5")
+    state = make_lattice(g, charged=True)
+    seeds = g.meta["chain_seeds"]
+    sampling = SweepSampling(state, g.cut, None, None, chains=len(seeds), seeds=seeds)
+    sampling.configuration.import_configuration(g.neel()[:, :, None])
+    for _ in range(3 * len(seeds)):
+        sampling()
+    observer = Observer(state, enable_energy=True, enable_gradient=True, enable_natural_gradient=True)
+    with observer:
+        for _ in range(5 * len(seeds)):
+            possibility, configuration = sampling()
+            observer(possibility, configuration)
+    eng = observer._engine
+    n = eng.holes_count()
+    H = np.stack([eng.holes_gemv(np.eye(n)[j], transpose=True) for j in range(n)])
+    G = eng.holes_gram()
+    np.testing.assert_allclose(G, H @ H.T, rtol=1e-12, atol=1e-12 * np.abs(H @ H.T).max())
+    r_pinv, a_pinv = 1e-6, 1e-9
+    x = np.concatenate([a.ravel() for row in observer.natural_gradient_by_direct_pseudo_inverse(r_pinv, a_pinv)
+                        for a in row])
+    scal = observer._read()
+    delta = np.asarray(observer._delta) / scal[1]
+    D = H - delta
+    E = np.asarray(observer._samples_e) - scal[4] / scal[1]
+    L, U = np.linalg.eigh(D @ D.T)
+    num = r_pinv * L.max() + a_pinv
+    Linv = np.array([0.0 if l <= 0 else 1.0 / (l * (1 + (num / l)**6)) for l in L])
+    want = 2 * D.T @ (U @ (Linv * (U.T @ E)))
+    np.testing.assert_allclose(x, want, rtol=0, atol=1e-8 * np.abs(want).max())

@@ -152,6 +152,9 @@ class _FakeEngine:
     def holes_gemv(self, x, transpose=False):
         return self.rows.T @ x if transpose else self.rows @ x
 
+    def holes_gram(self):
+        return self.rows @ self.rows.T
+
 
 class _FakeOwner:
     site_number = 1

@@ -41,6 +41,7 @@ SIGNATURES = {
     "tnsp_holes_keep": (ctypes.c_int, [_c_void_p, ctypes.c_int]),
     "tnsp_holes_count": (ctypes.c_int, [_c_void_p, _c_i64_p]),
     "tnsp_holes_gemv": (ctypes.c_int, [_c_void_p, ctypes.c_int, _c_dbl_p, _c_dbl_p]),
+    "tnsp_holes_gram": (ctypes.c_int, [_c_void_p, _c_dbl_p]),
     "tnsp_ctx_destroy": (ctypes.c_int, [_c_void_p]),
     "tnsp_last_error": (ctypes.c_char_p, [_c_void_p]),
     "tnsp_lattice_upload": (ctypes.c_int,

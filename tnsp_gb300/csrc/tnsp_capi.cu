@@ -46,6 +46,35 @@ __global__ void holes_gemv_rows(const double* __restrict__ H, long long np, long
 }
 
 // y[p] = sum_s H[s][p] u[s]: one thread per parameter, rows in order (coalesced along a row)
+// G = H H^T over the kept hole rows (rows x np, row-major): one 32 x 32 tile of G per block of 32 x 8
+// threads, the rows of both tiles staged in shared memory 32 parameters at a time; each thread
+// accumulates four entries of its column (float64, the parameters in order).
+__global__ void holes_gram(const double* __restrict__ H, long long np, long long rows, double* __restrict__ G) {
+  __shared__ double a[32][33], b[32][33];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const long long i0 = (long long)blockIdx.y * 32, j0 = (long long)blockIdx.x * 32;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (long long k0 = 0; k0 < np; k0 += 32) {
+    for (int r = ty; r < 32; r += 8) {
+      const long long k = k0 + tx;
+      a[r][tx] = (i0 + r < rows && k < np) ? H[(i0 + r) * np + k] : 0.0;
+      b[r][tx] = (j0 + r < rows && k < np) ? H[(j0 + r) * np + k] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int c = 0; c < 32; ++c) {
+      const double bv = b[tx][c];
+#pragma unroll
+      for (int m = 0; m < 4; ++m) acc[m] = fma(a[ty + 8 * m][c], bv, acc[m]);
+    }
+    __syncthreads();
+  }
+  for (int m = 0; m < 4; ++m) {
+    const long long i = i0 + ty + 8 * m, j = j0 + tx;
+    if (i < rows && j < rows) G[i * rows + j] = acc[m];
+  }
+}
+
 __global__ void holes_gemv_cols(const double* __restrict__ H, long long np, long long rows, const double* __restrict__ u,
                                 double* __restrict__ y) {
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < np; p += (long long)gridDim.x * blockDim.x) {
@@ -1025,6 +1054,28 @@ int tnsp_holes_gemv(tnsp_ctx* ctx, int transpose, const double* x, double* y) {
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(y, dy, sizeof(double) * (size_t)ny, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  return TNSP_OK;
+}
+
+int tnsp_holes_gram(tnsp_ctx* ctx, double* gram) {
+  if (!ctx || !gram) return TNSP_E_ARG;
+  if (!ctx->holes_rows) return fail(ctx, TNSP_E_STATE, "no hole rows kept (tnsp_holes_keep before an observed sweep)");
+  CK(cudaSetDevice(ctx->device));
+  const long long rows = ctx->holes_rows, np = ctx->n_params;
+  double* dg = nullptr;
+  CK(cudaMalloc((void**)&dg, sizeof(double) * (size_t)rows * rows));
+  const long long tiles = (rows + 31) / 32;
+  if (tiles > 65535) {
+    cudaFree(dg);
+    return fail(ctx, TNSP_E_ARG, "too many kept hole rows for the Gram product");
+  }
+  holes_gram<<<dim3((unsigned)tiles, (unsigned)tiles), dim3(32, 8), 0, ctx->stream>>>(ctx->d_holes, np, rows, dg);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(gram, dg, sizeof(double) * (size_t)rows * rows, cudaMemcpyDeviceToHost,
+                                            ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(dg);
+  CK(e);
   return TNSP_OK;
 }
 

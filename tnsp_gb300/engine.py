@@ -180,6 +180,13 @@ class Sampler:
                                              ptr(y, ctypes.c_double)), "tnsp_holes_gemv")
         return y
 
+    def holes_gram(self):
+        """H H^T over the kept hole rows (rows x rows), one device product."""
+        n = self.holes_count()
+        g = np.zeros((n, n))
+        self._check(self.lib.tnsp_holes_gram(self.ctx, ptr(g, ctypes.c_double)), "tnsp_holes_gram")
+        return g
+
     def read_samples(self, nsweeps):
         eloc = np.zeros((nsweeps, self.B))
         logws = np.zeros((nsweeps, self.B))

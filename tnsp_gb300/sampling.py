@@ -460,8 +460,8 @@ class Observer:
         equation of its single-process form (observer.py:902-907): with D_s = delta_s - <delta> over the
         kept samples (unweighted rows) and E_s = E_loc,s - <E>, T = D D^T = U diag(L) U^T,
         L^+ = 1 / (L (1 + ((r_pinv max L + a_pinv) / L)^6)) for L > 0 (0 otherwise), and the result
-        2 D^T U L^+ U^T E per site.  T is built from products with the rows kept on the device
-        (``tnsp_holes_gemv``); the reference distributes the samples with ScaLAPACK, so several ranks
+        2 D^T U L^+ U^T E per site.  T is built from the rows kept on the device: H H^T in one product
+        (``tnsp_holes_gram``) and the mean correction with H delta (``tnsp_holes_gemv``); the reference distributes the samples with ScaLAPACK, so several ranks
         raise NotImplementedError here (use the conjugate gradient).  ``libraries`` is accepted and not
         used."""
         if not self._enable_natural:
@@ -474,14 +474,9 @@ class Observer:
         delta = np.asarray(self._delta) / W
         En = np.asarray(self._samples_e) - scal[4] / W
         eng = self._engine
-        n = len(En)
-        T = np.empty((n, n))
-        unit = np.zeros(n)
-        for j in range(n):
-            unit[j] = 1.0
-            col = eng.holes_gemv(unit, transpose=True) - delta      # D^T e_j
-            T[:, j] = eng.holes_gemv(col) - np.dot(delta, col)       # D D^T e_j
-            unit[j] = 0.0
+        # T = D D^T with D = H - 1 delta^T: H H^T in one device product, then the mean correction
+        u = eng.holes_gemv(delta)                                     # H delta
+        T = eng.holes_gram() - u[:, None] - u[None, :] + np.dot(delta, delta)
         T = 0.5 * (T + T.T)
         L, U = np.linalg.eigh(T)
         num = r_pinv * L[-1] + a_pinv
