@@ -441,6 +441,65 @@ def run_observe_case(name, kind, L1, L2, D, cut, tensor_seed, chain_seeds, n_the
     print(f"{name}: observer set of {k} terms, saved {os.path.getsize(path)} bytes")
 
 
+def run_offdiag_case(name, kind, L1, L2, D, cut, tensor_seed, chain_seeds, n_therm, n_samples):
+    """The chains of case ``name`` observed with an ``observer_set`` of long-range operators with
+    off-diagonal elements (Sx on one site, SxSx and SS = SxSx + SySy + SzSz on distant pairs;
+    tetragono/tetragono/common_tensor/No.py), which the reference evaluates through its
+    ConfigurationPool (``cache_configuration=True``, observer.py:325-331, 368-369; lattice.py:473-696);
+    saves ``result`` / ``whole_result``, the operators' element tables and, per observed sample, the
+    configuration and its weight to <name>_offdiag.npz."""
+    lattice = build_lattice(kind, L1, L2, D, tensor_seed)
+    No = tet.common_tensor.No
+    Sx, SxSx, SS = No.Sx.to(float), No.SxSx.to(float), No.SS.to(float)
+    observer_set = {
+        "SxSx": {((0, 0, 0), (2, 2, 0)): SxSx, ((0, 1, 0), (2, 1, 0)): SxSx},
+        "SS": {((1, 0, 0), (1, 2, 0)): SS, ((0, 0, 0), (1, 1, 0)): SS},
+        "Sx": {((1, 1, 0),): Sx},
+    }
+    neel = np.zeros((L1, L2, 1), dtype=np.int64)
+    for l1 in range(L1):
+        for l2 in range(L2):
+            neel[l1, l2, 0] = (l1 + l2) % 2
+    observer = tet.Observer(lattice, observer_set={k: dict(v) for k, v in observer_set.items()}, enable_energy=True,
+                            cache_configuration=True)
+    phys = lattice.physics_edges[0, 0, 0]
+    confs, weights = [], []
+    with observer:
+        for seed in chain_seeds:
+            TAT.random.seed(seed)
+            sampling = tet.SweepSampling(lattice, cut, None, None)
+            sampling.configuration.import_configuration(neel)
+            for step in range(n_therm + n_samples):
+                possibility, configuration = sampling()
+                if step >= n_therm:
+                    observer(possibility, configuration)
+                    ws = float(configuration.hole(()))
+                    confs.append([[point_index(phys, configuration[l1, l2, 0]) for l2 in range(L2)]
+                                  for l1 in range(L1)])
+                    weights.append(ws * ws / possibility)
+    out, meta = {"confs": np.array(confs), "weights": np.array(weights)}, {"names": [], "positions": []}
+    result, whole = observer.result, observer.whole_result
+    k = 0
+    for nm, terms in observer_set.items():
+        for positions, H in terms.items():
+            rows = []
+            for s_in, outs in tensor_element(H).items():
+                for s_out, value in outs.items():
+                    rows.append([point_index(phys, p) for p in s_in] + [point_index(phys, p) for p in s_out] +
+                                [float(value.storage[0])])
+            out[f"table_{k}"] = np.array(rows)
+            out[f"result_{k}"] = np.array(result[nm][positions])
+            meta["names"].append(nm)
+            meta["positions"].append([list(p) for p in positions])
+            k += 1
+        out[f"whole_{nm}"] = np.array(whole[nm])
+    out["energy"] = np.array(observer.energy)
+    out["meta"] = np.array(json.dumps(meta))
+    path = os.path.join(HERE, f"{name}_offdiag.npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: off-diagonal observer set of {k} terms, saved {os.path.getsize(path)} bytes")
+
+
 def run_ergodic_case(name, kind, L1, L2, D, cut, tensor_seed):
     """The reference's ErgodicSampling (tetragono/tetragono/sampling_lattice/sampling.py:196-249) over every
     configuration of the lattice of case ``name`` with an energy Observer: the exact energy of the
@@ -471,6 +530,9 @@ def _pack_holes(holes, L1, L2):
     return [[dense_site(holes[l1][l2]) for l2 in range(L2)] for l1 in range(L1)]
 
 
+if __name__ == "__main__" and "--offdiag" in sys.argv:
+    run_offdiag_case("heis_no_3x3_D3_dc4", "no", 3, 3, 3, 4, 1234, [11, 12], 3, 5)
+    sys.exit(0)
 if __name__ == "__main__" and "--restricted" in sys.argv:
     run_restricted_case("heis_no_3x3_D3_dc4_restricted", "heis_no_3x3_D3_dc4", "no", 3, 3, 3, 4, 1234, [11, 12], 3, 5)
     sys.exit(0)

@@ -162,3 +162,37 @@ def test_hole_row_gram_product_and_pseudo_inverse():
     Linv = np.array([0.0 if l <= 0 else 1.0 / (l * (1 + (num / l)**6)) for l in L])
     want = 2 * D.T @ (U @ (Linv * (U.T @ E)))
     np.testing.assert_allclose(x, want, rtol=0, atol=1e-8 * np.abs(want).max())
+
+
+def test_off_diagonal_observer_set_matches_reference():
+    """Long-range operators with off-diagonal elements (Sx, SxSx and SS at distance 2) observed in the
+    driver loop: the replaced configurations' amplitudes come from the device amplitude entry, against
+    the reference's ConfigurationPool results on the same chains
+    (tests/golden/heis_no_3x3_D3_dc4_offdiag.npz)."""
+    import json
+    import os
+    from golden_cases import GOLDEN
+    from test_gpu_parity import make_lattice
+    from test_observer_set import _tables
+    from tnsp_gb300.sampling import Observer, SweepSampling
+    g = Golden("heis_no_3x3_D3_dc4")
+    z = np.load(os.path.join(GOLDEN, "heis_no_3x3_D3_dc4_offdiag.npz"))
+    meta = json.loads(str(z["meta"]))
+    state = make_lattice(g, charged=True)
+    seeds = g.meta["chain_seeds"]
+    nt, ns = g.meta["n_therm"], g.meta["n_samples"]
+    sampling = SweepSampling(state, g.cut, None, None, chains=len(seeds), seeds=seeds)
+    sampling.configuration.import_configuration(g.neel()[:, :, None])
+    for _ in range(nt * len(seeds)):
+        sampling()
+    observer = Observer(state, observer_set=_tables(z, meta), enable_energy=True, cache_configuration=True)
+    with observer:
+        for _ in range(ns * len(seeds)):
+            observer(*sampling())
+    result, whole = observer.result, observer.whole_result
+    for k, (name, positions) in enumerate(zip(meta["names"], meta["positions"])):
+        np.testing.assert_allclose(result[name][tuple(tuple(p) for p in positions)], z[f"result_{k}"], rtol=1e-10,
+                                   atol=1e-13)
+    for name in set(meta["names"]):
+        np.testing.assert_allclose(whole[name], z[f"whole_{name}"], rtol=1e-10, atol=1e-13)
+    np.testing.assert_allclose(observer.energy[0], z["energy"][0], rtol=1e-10)

@@ -222,7 +222,7 @@ def _observer_set_worker(rank, world, port, q):
     obs = Observer(_FakeOwner3(), observer_set=sets, enable_energy=True)
     obs.__enter__()
     obs._bind(_FakeEngine(np.zeros((len(w[mine]), 1)), w[mine], e[mine]))
-    obs._observe_diagonal(confs[mine], w[mine])
+    obs._observe_set(confs[mine], w[mine])
     obs.__exit__(None, None, None)
     res = obs.result
     q.put((rank, {n: {str(k): v for k, v in d.items()} for n, d in res.items()}, obs.whole_result))
@@ -266,7 +266,7 @@ def test_two_rank_observer_set_equals_one_process():
     one = Observer(_FakeOwner3(), observer_set=sets, enable_energy=True)
     one.__enter__()
     one._bind(_FakeEngine(np.zeros((len(w), 1)), w, e))
-    one._observe_diagonal(confs, w)
+    one._observe_set(confs, w)
     one.__exit__(None, None, None)
     want = {n: {str(k): v for k, v in d.items()} for n, d in one.result.items()}
     for rank, res, whole in out:

@@ -59,7 +59,7 @@ def test_diagonal_observer_set_matches_reference():
     obs.__enter__()
     obs._bind(_Engine(scalars))
     for c, rw in zip(confs, w):
-        obs._observe_diagonal([c], [rw])
+        obs._observe_set([c], [rw])
     obs.__exit__(None, None, None)
     result, whole = obs.result, obs.whole_result
     for k, (name, positions) in enumerate(zip(meta["names"], meta["positions"])):
@@ -70,7 +70,79 @@ def test_diagonal_observer_set_matches_reference():
     np.testing.assert_allclose(whole["energy"], np.array(z["energy"]) * 9, rtol=1e-10)  # total = 9 x per site
 
 
-def test_off_diagonal_observers_are_refused():
-    flip = {(0, 1): [((1, 0), 0.5)], (1, 0): [((0, 1), 0.5)]}
-    with pytest.raises(NotImplementedError):
-        Observer(_Owner(), observer_set={"flip": {((0, 0, 0), (2, 2, 0)): flip}})
+class _AmplitudeEngine(_Engine):
+    """A stand-in engine whose ``amplitude`` is the oracle's hole(()) (oracle/peps_oracle.py), as the
+    device amplitude entry returns it (mantissa, exponent)."""
+
+    def __init__(self, scalars, peps):
+        super().__init__(scalars)
+        self.peps = peps
+        self.calls = 0
+
+    def amplitude(self, configs):
+        from oracle.peps_oracle import Environment
+        self.calls += 1
+        m = np.array([Environment(self.peps, c).amplitude() for c in np.asarray(configs)])
+        return m, np.zeros(len(m), dtype=np.int32)
+
+
+def _oracle_peps(name):
+    from golden_cases import Golden
+    from oracle.peps_oracle import DensePEPS
+    g = Golden(name)
+    return DensePEPS(g.dense_sites(), g.terms(), g.cut)
+
+
+def test_off_diagonal_observer_set_matches_reference():
+    """Off-diagonal long-range operators (Sx, SxSx, SS at distance 2) on the golden chains: the drop-in
+    Observer's per-sample values from replaced configurations' amplitudes (here the oracle's, on the
+    device the amplitude kernel's) against the reference's ConfigurationPool results
+    (tests/golden/heis_no_3x3_D3_dc4_offdiag.npz)."""
+    z = np.load(os.path.join(GOLDEN, "heis_no_3x3_D3_dc4_offdiag.npz"))
+    meta = json.loads(str(z["meta"]))
+    confs, w = z["confs"], z["weights"]
+    scalars = np.array([len(w), w.sum(), (w * w).sum(), 0.0, 0.0, 0.0, 0.0, 0])
+    engine = _AmplitudeEngine(scalars, _oracle_peps("heis_no_3x3_D3_dc4"))
+    obs = Observer(_Owner(), observer_set=_tables(z, meta), enable_energy=True, cache_configuration=True)
+    obs.__enter__()
+    obs._bind(engine)
+    obs._observe_set(confs[:7], w[:7])  # two sweeps' worth of samples, amplitudes batched per sweep
+    obs._observe_set(confs[7:], w[7:])
+    obs.__exit__(None, None, None)
+    assert engine.calls == 4
+    result, whole = obs.result, obs.whole_result
+    for k, (name, positions) in enumerate(zip(meta["names"], meta["positions"])):
+        np.testing.assert_allclose(result[name][tuple(tuple(p) for p in positions)], z[f"result_{k}"], rtol=1e-10,
+                                   atol=1e-13)
+    for name in set(meta["names"]):
+        np.testing.assert_allclose(whole[name], z[f"whole_{name}"], rtol=1e-10, atol=1e-13)
+
+
+def test_off_diagonal_observers_respect_the_restriction():
+    """A restriction that forbids changing site (1, 1) (observer.py:364-367, asked for every element,
+    the diagonal one included): Sx there vanishes, SS across it keeps only its diagonal SzSz part, and
+    terms away from it keep the reference's values."""
+    z = np.load(os.path.join(GOLDEN, "heis_no_3x3_D3_dc4_offdiag.npz"))
+    meta = json.loads(str(z["meta"]))
+    confs, w = z["confs"], z["weights"]
+    scalars = np.array([len(w), w.sum(), (w * w).sum(), 0.0, 0.0, 0.0, 0.0, 0])
+    engine = _AmplitudeEngine(scalars, _oracle_peps("heis_no_3x3_D3_dc4"))
+    owner = _Owner()
+    owner.P, owner.charges = 2, None
+
+    def fixed_center(configuration, replacement):
+        return all(configuration[p] == v for p, v in replacement.items() if p == (1, 1, 0))
+
+    obs = Observer(owner, observer_set=_tables(z, meta), enable_energy=True, restrict_subspace=fixed_center)
+    obs.__enter__()
+    obs._engine = engine  # bound without the device-side energy restriction
+    obs._observe_set(confs, w)
+    obs.__exit__(None, None, None)
+    result = obs.result
+    assert result["Sx"][((1, 1, 0),)] == (0.0, 0.0)
+    szsz = (0.5 - confs[:, 0, 0]) * (0.5 - confs[:, 1, 1])
+    np.testing.assert_allclose(result["SS"][((0, 0, 0), (1, 1, 0))][0], (szsz * w).sum() / w.sum(), rtol=1e-12)
+    for k, (name, positions) in enumerate(zip(meta["names"], meta["positions"])):
+        positions = tuple(tuple(p) for p in positions)
+        if (1, 1, 0) not in positions:
+            np.testing.assert_allclose(result[name][positions], z[f"result_{k}"], rtol=1e-10, atol=1e-13)

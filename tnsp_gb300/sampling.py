@@ -20,8 +20,9 @@ accumulators.
 Only the features of the sweep / E_loc / gradient / natural-gradient path are mirrored.  Restricted
 subspaces and custom hopping Hamiltonians are accepted when the restriction depends on the replaced
 sites only (as tetraku's ``restrict_Sz`` does): it is evaluated here for every table entry and the
-device skips the disallowed ones.  No cached deltas or configurations, no off-diagonal observer sets
-(``NotImplementedError`` where the reference would accept them).
+device skips the disallowed ones.  Observer sets take diagonal and off-diagonal operators at any
+distance (the replaced configurations' amplitudes come from the device amplitude entry).  No cached
+deltas (``NotImplementedError`` where the reference would accept them).
 """
 import numpy as np
 
@@ -217,7 +218,7 @@ class SweepSampling:
                     observer._samples_e.extend(eloc[0].tolist())
                     observer._samples_w.extend(reweight[0].tolist())
                 if observer._observer_set:
-                    observer._observe_diagonal(conf, reweight[0])
+                    observer._observe_set(conf, reweight[0])
             self._buffer = [(float(np.exp(lp)), Configuration(self.owner, c), observing) for c, lp in zip(conf, logp)]
             self._buffer.reverse()
         possibility, configuration, observed = self._buffer.pop()
@@ -232,15 +233,19 @@ class Observer:
     def __init__(self, owner, *, observer_set=None, enable_energy=False, enable_gradient=False,
                  enable_natural_gradient=False, cache_natural_delta=None, cache_configuration=False,
                  restrict_subspace=None, classical_energy=None):
-        if cache_natural_delta or cache_configuration or classical_energy is not None:
-            raise NotImplementedError("only energy, gradient, natural-gradient and diagonal observer-set observation "
-                                      "are supported")
+        # cache_configuration (True or "drop") selects the reference's ConfigurationPool for replaced
+        # amplitudes; here they always come from the amplitude entry, so it changes nothing
+        if cache_natural_delta or classical_energy is not None:
+            raise NotImplementedError("cached natural-gradient deltas and classical energies are not supported")
         self.owner = owner
         self._restrict = restrict_subspace
         # observer_set: {name: {positions: element table}}, tables as the lattice's Hamiltonian tables
-        # ({input tuple: [(output tuple, value)]}); diagonal operators only (their value needs the sampled
-        # configuration alone, as Sz or n at any distance)
+        # ({input tuple: [(output tuple, value)]}).  Diagonal elements need the sampled configuration
+        # alone; off-diagonal ones need the amplitude of the replaced configuration at any distance,
+        # which the reference takes from its ConfigurationPool (lattice.py:473-696) and this observer from
+        # the device amplitude entry (tnsp_amplitude) for all samples of a sweep at once
         self._observer_set = {}
+        self._has_offdiag = False
         for name, terms in (observer_set or {}).items():
             if name == "energy":
                 raise ValueError("the name 'energy' is reserved for the Hamiltonian")
@@ -249,15 +254,18 @@ class Observer:
                 positions = tuple(tuple(p) for p in positions)
                 if any(p[2] != 0 for p in positions):
                     raise NotImplementedError("only orbit 0 is supported")
-                diag = {}
+                diag, off = {}, {}
                 for s_in, outs in table.items():
                     for s_out, value in outs:
-                        if tuple(s_out) != tuple(s_in):
-                            raise NotImplementedError(f"observer '{name}' at {positions}: off-diagonal elements need "
-                                                      "replacement amplitudes, which are not supported")
-                        diag[tuple(s_in)] = diag.get(tuple(s_in), 0.0) + float(value)
-                entries.append((positions, diag))
+                        if tuple(s_out) == tuple(s_in):
+                            diag[tuple(s_in)] = diag.get(tuple(s_in), 0.0) + float(value)
+                        else:
+                            off.setdefault(tuple(s_in), []).append((tuple(s_out), float(value)))
+                self._has_offdiag |= bool(off)
+                entries.append((positions, diag, off))
             self._observer_set[name] = entries
+        if self._has_offdiag and getattr(owner, "fermion", None) is not None:
+            raise NotImplementedError("off-diagonal observer sets on fermionic lattices")
         self._set_acc = None
         self._enable_natural = bool(enable_natural_gradient)
         self._enable_energy = enable_energy or enable_gradient or self._enable_natural
@@ -282,19 +290,65 @@ class Observer:
         self.owner._active_observer = self
         return self
 
-    def _observe_diagonal(self, confs, reweights):
-        """Observer.__call__ (observer.py:344-402) for the diagonal observer set: per sample with nonzero
-        weight w and per term the value x = <s|O|s>, summing x w, x w^2 and x^2 w^2, and the same for the
-        sum over a name's terms."""
-        for conf, w in zip(confs, reweights):
-            if w == 0.0:
+    def _allowed(self, conf, positions, s_out):
+        """restrict_subspace(configuration, replacement) of the observer (observer.py:364-367)."""
+        if self._restrict is None:
+            return True
+        charges = getattr(self.owner, "charges", None)
+        ch = list(charges[1]) if charges is not None else [0] * self.owner.P
+        replacement = {p: _edge_point(ch, int(v)) for p, v in zip(positions, s_out)}
+        return bool(self._restrict(_RestrictionView(self.owner, conf, ch), replacement))
+
+    def _offdiag_values(self, confs, keep):
+        """Per kept sample i and term (name, k): sum over s' != s of <s'|O|s> psi(s') / psi(s)
+        (observer.py:355-389), with psi of the sample and of every replaced configuration from the
+        amplitude kernel; terms the observer's restriction forbids (observer.py:364-367) and replaced
+        configurations of zero amplitude contribute nothing."""
+        requests, replaced = [], []
+        for i, b in enumerate(keep):
+            conf = confs[b]
+            for name, entries in self._observer_set.items():
+                for k, (positions, _, off) in enumerate(entries):
+                    outs = off.get(tuple(int(conf[p[0], p[1]]) for p in positions))
+                    if not outs:
+                        continue
+                    for s_out, value in outs:
+                        if not self._allowed(conf, positions, s_out):
+                            continue
+                        c = conf.copy()
+                        for p, v in zip(positions, s_out):
+                            c[p[0], p[1]] = v
+                        requests.append((i, name, k, value))
+                        replaced.append(c)
+        values = {}
+        if not replaced:
+            return values
+        m0, e0 = self._engine.amplitude(confs[keep])
+        m1, e1 = self._engine.amplitude(np.array(replaced))
+        for (i, name, k, value), mm, ee in zip(requests, m1, e1):
+            if m0[i] == 0.0 or mm == 0.0:
                 continue
-            conf = np.asarray(conf).reshape(self.owner.L1, self.owner.L2)
+            values[(i, name, k)] = values.get((i, name, k), 0.0) + value * float(np.ldexp(mm / m0[i], int(ee - e0[i])))
+        return values
+
+    def _observe_set(self, confs, reweights):
+        """Observer.__call__ (observer.py:344-402) for the observer set: per sample with nonzero weight w
+        and per term the value x = sum over s' of <s'|O|s> psi(s') / psi(s), summing x w, x w^2 and
+        x^2 w^2, and the same for the sum over a name's terms."""
+        confs = np.asarray(confs).reshape(-1, self.owner.L1, self.owner.L2)
+        keep = [b for b in range(len(confs)) if reweights[b] != 0.0]
+        off = self._offdiag_values(confs, keep) if (self._has_offdiag and keep) else {}
+        for i, b in enumerate(keep):
+            conf, w = confs[b], reweights[b]
             for name, entries in self._observer_set.items():
                 acc, whole = self._set_acc[name]
                 total = 0.0
-                for k, (positions, diag) in enumerate(entries):
-                    x = diag.get(tuple(int(conf[p[0], p[1]]) for p in positions), 0.0)
+                for k, (positions, diag, _) in enumerate(entries):
+                    s_in = tuple(int(conf[p[0], p[1]]) for p in positions)
+                    x = diag.get(s_in, 0.0)
+                    if x != 0.0 and not self._allowed(conf, positions, s_in):
+                        x = 0.0  # the reference asks the restriction about the unchanged sites as well
+                    x += off.get((i, name, k), 0.0)
                     acc[k] += (x * w, x * w * w, x * x * w * w)
                     total += x
                 whole += (total * w, total * w * w, total * total * w * w)
@@ -349,8 +403,7 @@ class Observer:
     @property
     def result(self):
         """``Observer.result``: {name: {positions: (expect, deviation)}} of the observer set."""
-        return {name: {positions: self._expect(self._set_acc[name][0][k])
-                       for k, (positions, _) in enumerate(entries)}
+        return {name: {entry[0]: self._expect(self._set_acc[name][0][k]) for k, entry in enumerate(entries)}
                 for name, entries in self._observer_set.items()}
 
     @property
