@@ -298,13 +298,17 @@ def dist_setup(gpus):
     return rank, world, dist
 
 
-def _sampler(w, lat, local, precision, B, seeds, tune=False):
-    """A Sampler with B chains of the workload (B <= 0: one resident wave), started by chain_starts."""
+def _sampler(w, lat, local, precision, B, seeds, tune=False, blocks_per_sm=0):
+    """A Sampler with B chains of the workload (B <= 0: one resident wave), started by chain_starts;
+    blocks_per_sm > 0 fixes the thread blocks (chains) resident per SM instead of the library's choice."""
     from tnsp_gb300.engine import Sampler
+    from tnsp_gb300._lib import TNSP_OPT_BLOCKS_PER_SM
     s = Sampler(lat, w["cut"], device=local)
     first = _first_filling(w, lat)
     s.init_chains(first[None], seeds[:1], precision=precision)
-    if tune:
+    if blocks_per_sm > 0:
+        s.set_option(TNSP_OPT_BLOCKS_PER_SM, blocks_per_sm)
+    elif tune:
         from tnsp_gb300.autotune import tune_blocks_per_sm
         tune_blocks_per_sm(s, first[None], device=local)
     # plan for as many chains as the device holds at once (the library caps the slots it allocates)
@@ -394,7 +398,7 @@ def run_ours(args):
     lat = make_lattice(w)
     prec = PRECISIONS[args.precision]
     s, B, seeds = _sampler(w, lat, local, prec, args.chains or w["chains"],
-                           np.array([7919 * (rank + 1)], dtype=np.uint64))
+                           np.array([7919 * (rank + 1)], dtype=np.uint64), blocks_per_sm=args.blocks_per_sm)
     t_setup = time.perf_counter()
     s.sweep(w["therm"])
     therm_s = time.perf_counter() - t_setup
@@ -489,6 +493,7 @@ def run_ours(args):
         "data": "synthetic (seeded random PEPS; " + ("random fillings" if w["kind"] == "tv" else "Neel start") + ")",
         "config": {"workload": args.workload, "statement": w["config"], "lattice": f"{w['L1']}x{w['L2']}", "D": w["D"],
                    "sectors": w.get("sectors"), "Dcut": w["cut"], "precision": args.precision, "chains_per_gpu": B,
+                   "blocks_per_sm": args.blocks_per_sm or "library default",
                    "resident_chains": resident, "thermalisation_sweeps": w["therm"],
                    "parallelism": f"replicas{world}", "l2": "working set larger than L2 (per-chain scratch slots)"},
         "raw_samples_per_s": raw,
@@ -713,6 +718,7 @@ def main():
                     choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(PROPOSAL_WORKLOADS))
     ap.add_argument("--precision", default="", choices=["", "fp64", "dd", "fp32", "mixed"], help="default: per workload")
     ap.add_argument("--chains", type=int, default=0)
+    ap.add_argument("--blocks-per-sm", type=int, default=0, help="chains resident per SM (default: the library's)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--train-sweeps", type=int, default=10, help="learned proposal: plain sweeps of training data")
