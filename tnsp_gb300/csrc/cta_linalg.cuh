@@ -368,6 +368,199 @@ template <class T> __device__ void block_orgqr_cm(int m, int k, T* G, const T* t
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// blocked Householder QR for matrices staged in global memory (compact WY form of a panel:
+// H_0 H_1 ... H_{b-1} = I - V Tw V^T, LAPACK larft / larfb)
+// ---------------------------------------------------------------------------------------------
+// The unblocked routines above read and write the whole trailing matrix once per reflector; from
+// global memory that is one latency-bound pass per column.  The panel routines factorise (or form)
+// up to kNB columns at a time in shared memory and apply them to the rest of the matrix as one block
+// reflector: two reads and one write of each trailing column per panel, with kNB independent dot
+// products per lane in flight.  Results equal the unblocked ones up to rounding (same reflectors).
+constexpr int kNB = 8;
+
+// Tw (jb x jb upper triangular, row stride kNB) of the explicit unit-lower panel V (pm x jb,
+// column-major, ld pm; zeros above the unit diagonal) and its scalars tau:
+//   Tw[i][i] = tau_i,   Tw[0:i][i] = -tau_i Tw[0:i][0:i] (V[:, 0:i]^T v_i).
+// Y (kNB x kNB) is scratch for the Gram entries v_a . v_b, a < b.  Both live in shared memory.
+template <class T> __device__ void panel_tw(int pm, int jb, const T* V, const T* tau, T* Y, T* Tw) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, grp = lane / kJG, sl = lane % kJG;
+  const int npairs = jb * (jb - 1) / 2;
+  for (int base = w * (32 / kJG); base < npairs; base += kWarps * (32 / kJG)) {  // warp-uniform
+    const int p = base + grp;
+    const bool act = p < npairs;
+    int a = 0, b = 1;
+    if (act) {  // pairs enumerated by b = 1, 2, ... with a = 0 .. b-1
+      int q = p;
+      while (q >= b) {
+        q -= b;
+        ++b;
+      }
+      a = q;
+    }
+    T d = 0;
+    if (act)  // v_b is zero above row b and 1 at it: the overlap starts at row b
+      for (int r = b + sl; r < pm; r += kJG) d = fma(V[(long)a * pm + r], V[(long)b * pm + r], d);
+    d = group_sum<kJG>(d);
+    if (act && sl == 0) Y[a * kNB + b] = d;
+  }
+  __syncthreads();
+  // column i of Tw from its columns < i; lane a owns row a (it reads only its own row and Y)
+  if (threadIdx.x < 32) {
+    for (int i = 0; i < jb; ++i) {
+      if (lane < i) {
+        T s = 0;
+        for (int c = lane; c < i; ++c) s = fma(Tw[lane * kNB + c], Y[c * kNB + i], s);
+        Tw[lane * kNB + i] = -tau[i] * s;
+      } else if (lane == i) {
+        Tw[i * kNB + i] = tau[i];
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// A <- (I - V op(Tw) V^T) A on columns c0..n-1 of A (pm rows, column-major, ld lda); op(Tw) = Tw^T
+// applies Q^T of the panel (the factorisation's trailing update), op(Tw) = Tw applies Q (forming Q).
+// One kJG-lane group per column.  No barrier at the end.
+template <class T, bool TRANS>
+__device__ void apply_panel(int pm, int jb, const T* V, const T* Tw, T* A, long lda, int c0, int n) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, grp = lane / kJG, sl = lane % kJG;
+  for (int base = c0 + w * (32 / kJG); base < n; base += kWarps * (32 / kJG)) {  // warp-uniform
+    const int c = base + grp;
+    const bool act = c < n;
+    T* ac = A + (long)(act ? c : base) * lda;
+    T y[kNB];
+#pragma unroll
+    for (int i = 0; i < kNB; ++i) y[i] = 0;
+    if (act)
+      for (int r = sl; r < pm; r += kJG) {
+        const T x = ac[r];
+#pragma unroll
+        for (int i = 0; i < kNB; ++i)
+          if (i < jb) y[i] = fma(V[(long)i * pm + r], x, y[i]);
+      }
+#pragma unroll
+    for (int i = 0; i < kNB; ++i) y[i] = group_sum<kJG>(y[i]);
+    // y <- op(Tw) y in place: Tw^T y (lower triangular) from the last entry down, Tw y (upper) up
+    if (TRANS) {
+#pragma unroll
+      for (int i = kNB - 1; i >= 0; --i) {
+        T s = 0;
+#pragma unroll
+        for (int a = 0; a <= i; ++a)
+          if (i < jb) s = fma(Tw[a * kNB + i], y[a], s);
+        y[i] = s;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < kNB; ++i) {
+        T s = 0;
+#pragma unroll
+        for (int b = i; b < kNB; ++b)
+          if (b < jb) s = fma(Tw[i * kNB + b], y[b], s);
+        y[i] = s;
+      }
+    }
+    if (act)
+      for (int r = sl; r < pm; r += kJG) {
+        T s = 0;
+#pragma unroll
+        for (int i = 0; i < kNB; ++i)
+          if (i < jb) s = fma(V[(long)i * pm + r], y[i], s);
+        ac[r] -= s;
+      }
+  }
+}
+
+// Panel width for an m-row matrix with pcap elements of shared staging (0 or 1: not blocked).
+__device__ __forceinline__ int panel_width(int m, long pcap) {
+  const long room = pcap - 2L * kNB * kNB;
+  if (m <= 0 || room < 2L * m) return 0;
+  return room / m < kNB ? (int)(room / m) : kNB;
+}
+
+// Copies the panel G[r0.., c0..c0+jb) (pm rows, G column-major with ld m) to P (ld pm) or back.
+template <class T> __device__ void panel_copy(int m, int pm, int jb, T* G, long goff, T* P, bool to_panel) {
+  for (long e = threadIdx.x; e < (long)pm * jb; e += blockDim.x) {
+    const int c = (int)(e / pm), r = (int)(e % pm);
+    T* g = G + goff + (long)c * m + r;
+    if (to_panel)
+      P[e] = *g;
+    else
+      *g = P[e];
+  }
+}
+
+// Zeros above the diagonal and ones on it: the explicit unit-lower V of a geqrf-layout panel.
+template <class T> __device__ void panel_explicit(int pm, int jb, T* P) {
+  for (int e = threadIdx.x; e < jb * jb; e += blockDim.x) {
+    const int c = e / jb, r = e % jb;
+    if (r <= c) P[(long)c * pm + r] = r == c ? (T)1 : (T)0;
+  }
+}
+
+// block_geqrf_cm for G in global memory, blocked through the shared staging P (pcap elements).
+template <class T> __device__ void block_geqrf_panel(int m, int n, T* G, T* tau, T* red, T* P, long pcap) {
+  const int nb = panel_width(m, pcap);
+  if (nb < 2) {
+    block_geqrf_cm(m, n, G, tau, red);
+    return;
+  }
+  const int kk = m < n ? m : n;
+  for (int j0 = 0; j0 < kk; j0 += nb) {
+    const int jb = kk - j0 < nb ? kk - j0 : nb, pm = m - j0;
+    const long goff = (long)j0 * m + j0;
+    T* Y = P + (long)pm * jb;
+    T* Tw = Y + kNB * kNB;
+    panel_copy(m, pm, jb, G, goff, P, true);
+    __syncthreads();
+    block_geqrf_cm(pm, jb, P, tau + j0, red);  // ends with a barrier
+    panel_copy(m, pm, jb, G, goff, P, false);  // R's rows of the panel and its reflectors
+    __syncthreads();
+    if (j0 + jb < n) {
+      panel_explicit(pm, jb, P);
+      __syncthreads();
+      panel_tw(pm, jb, P, tau + j0, Y, Tw);
+      apply_panel<T, true>(pm, jb, P, Tw, G + j0, m, j0 + jb, n);
+      __syncthreads();
+    }
+  }
+}
+
+// block_orgqr_cm for G in global memory, blocked through the shared staging P (pcap elements):
+// panels from the last one back, each applied to the columns already formed to its right and then
+// formed itself in shared memory.
+template <class T> __device__ void block_orgqr_panel(int m, int k, T* G, const T* tau, T* red, T* P, long pcap) {
+  const int nb = panel_width(m, pcap);
+  if (nb < 2) {
+    block_orgqr_cm(m, k, G, tau);
+    return;
+  }
+  for (int j0 = ((k - 1) / nb) * nb; j0 >= 0; j0 -= nb) {
+    const int jb = k - j0 < nb ? k - j0 : nb, pm = m - j0;
+    const long goff = (long)j0 * m + j0;
+    T* Y = P + (long)pm * jb;
+    T* Tw = Y + kNB * kNB;
+    panel_copy(m, pm, jb, G, goff, P, true);
+    __syncthreads();
+    panel_explicit(pm, jb, P);
+    __syncthreads();
+    if (j0 + jb < k) {
+      panel_tw(pm, jb, P, tau + j0, Y, Tw);
+      apply_panel<T, false>(pm, jb, P, Tw, G + j0, m, j0 + jb, k);
+      __syncthreads();
+    }
+    block_orgqr_cm(pm, jb, P, tau + j0);  // ends with a barrier
+    panel_copy(m, pm, jb, G, goff, P, false);
+    for (long e = threadIdx.x; e < (long)jb * j0; e += blockDim.x) {  // rows above the panel
+      const int c = (int)(e / j0), r = (int)(e % j0);
+      G[(long)(j0 + c) * m + r] = (T)0;
+    }
+    __syncthreads();
+  }
+}
+
 
 
 // ---------------------------------------------------------------------------------------------

@@ -1,4 +1,6 @@
 // double-float (dd) instantiation of the sampler kernels and its host launch wrappers.
+#include <mutex>
+
 #include "launch.h"
 
 namespace tnsp {
@@ -16,7 +18,14 @@ void launch_amplitude_dd(int grid, size_t smem, cudaStream_t st, const Model& md
                                                          out_m, out_e, status);
 }
 
+// The limit is a property of the kernel function, shared by every context of the process: it is only
+// ever raised, so a context planned with less dynamic shared memory never lowers it under another
+// context that launches with more.
 cudaError_t set_smem_limit_dd(int bytes) {
+  static std::mutex mu;
+  static int current = -1;
+  std::lock_guard<std::mutex> lock(mu);
+  if (bytes <= current) return cudaSuccess;
   cudaError_t e = cudaFuncSetAttribute(sweep_kernel<dd, dd>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(sweep_kernel<dd, dd>, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -26,6 +35,7 @@ cudaError_t set_smem_limit_dd(int bytes) {
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(amplitude_kernel<dd, dd>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              cudaSharedmemCarveoutMaxShared);
+  if (e == cudaSuccess) current = bytes;
   return e;
 }
 

@@ -1,4 +1,6 @@
 // float64 instantiation of the sampler kernels and its host launch wrappers.
+#include <mutex>
+
 #include "launch.h"
 
 namespace tnsp {
@@ -16,7 +18,14 @@ void launch_amplitude_f64(int grid, size_t smem, cudaStream_t st, const Model& m
                                                                  B, confs, out_m, out_e, status);
 }
 
+// The limit is a property of the kernel function, shared by every context of the process: it is only
+// ever raised, so a context planned with less dynamic shared memory never lowers it under another
+// context that launches with more.
 cudaError_t set_smem_limit_f64(int bytes) {
+  static std::mutex mu;
+  static int current = -1;
+  std::lock_guard<std::mutex> lock(mu);
+  if (bytes <= current) return cudaSuccess;
   cudaError_t e = cudaFuncSetAttribute(sweep_kernel<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(sweep_kernel<double, double>, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -26,6 +35,7 @@ cudaError_t set_smem_limit_f64(int bytes) {
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(amplitude_kernel<double, double>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              cudaSharedmemCarveoutMaxShared);
+  if (e == cudaSuccess) current = bytes;
   return e;
 }
 

@@ -792,7 +792,11 @@ template <class T, class S> struct Engine : Chain<T, S> {
         // the tensor's largest one inside the exponent range of float-based element types
         const int es = block_normalize(g, (long long)mr * mc, red);
         const T rsc = (T)ldexp(1.0, es);
-        block_geqrf_cm(mr, mc, g, tau, red);
+        // a sector staged in the slot is factorised in panels through the (then unused) shared memory
+        if (g == sm)
+          block_geqrf_cm(mr, mc, g, tau, red);
+        else
+          block_geqrf_panel(mr, mc, g, tau, red, sm, smcap);
         {
           const double mm = mr > mc ? mr : mc, nn = kr;
           this->count(1, 2.0 * (2.0 * mm * nn * nn - 2.0 * nn * nn * nn / 3.0));
@@ -804,7 +808,10 @@ template <class T, class S> struct Engine : Chain<T, S> {
           rb[e] = z >= y ? g[(long long)z * mr + y] * rsc : (T)0;
         }
         __syncthreads();
-        block_orgqr_cm(mr, kr, g, tau);
+        if (g == sm)
+          block_orgqr_cm(mr, kr, g, tau);
+        else
+          block_orgqr_panel(mr, kr, g, tau, red, sm, smcap);
         for (long long e = threadIdx.x; e < (long long)mr * kr; e += blockDim.x) {
           const int y = (int)(e / mr), x = (int)(e % mr);
           Tq[(long long)R_[x] * ktot + koff + y] = cvt<S>(g[e]);
@@ -823,29 +830,44 @@ template <class T, class S> struct Engine : Chain<T, S> {
       // of to the product (exact either way): the product is not read and written a second time
       expo += block_normalize(Rb, (long long)rsz, red);
       // new T[i+1] (ktot x d'B') = R * T[i+1], sector by sector, into G; each thread owns a 4x4
-      // output tile (4 rows of one sector's R x 4 columns), so one load of T feeds 4 FMAs
+      // output tile (4 rows of one sector's R x 4 columns), so one load of T feeds 4 FMAs.  The rows
+      // C_ of T[i+1] that a sector's R reads share one left charge, so only the columns (d', b') with
+      // charge F_{i+1} minus it can be nonzero in those rows (and in the sector's output rows): they
+      // are listed (in rl, free after the Q scatter) and only they are computed; G starts zeroed.
       const int dB = s_dd[i + 1] * s_dB[i + 1];
       {
         const S* Tn = Tbuf(s_buf[i + 1]);
-        const int tc = (dB + 3) / 4;
+        const int Bn = s_dB[i + 1], Fn = s_fl[i + 1];
+        const int* qLo = tqL(i + 1);  // left charges of T[i+1] before this step
+        const int* qDn = tqD(i + 1);
+        const int* qRn = tqR(i + 1);
+        for (long long e = threadIdx.x; e < (long long)ktot * dB; e += blockDim.x) G[e] = (S)0;
+        __syncthreads();
         int kof = 0;
+        double fl = 0;
         for (int t = 0; t < ns; ++t) {
           const int mc = s_sec.c[t], kr = min(s_sec.m[t], mc);
           const T* rb = Rb + s_roffs[t];
           const int* C_ = cl + s_sec.co[t];
-          const int tr = (kr + 3) / 4;
+          const int want = Fn - qLo[C_[0]];
+          const int nc = block_compact(
+              dB, [&](int col) { return qDn[col / Bn] + qRn[col % Bn] == want; }, rl, s_sh);
+          const int tr = (kr + 3) / 4, tc = (nc + 3) / 4;
           for (long long tile = threadIdx.x; tile < (long long)tr * tc; tile += blockDim.x) {
             const int y0 = (int)(tile / tc) * 4, c0 = (int)(tile % tc) * 4;
+            int col[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) col[u] = rl[c0 + u < nc ? c0 + u : nc - 1];
             S acc[4][4];
 #pragma unroll
             for (int v = 0; v < 4; ++v)
 #pragma unroll
               for (int u = 0; u < 4; ++u) acc[v][u] = (S)0;
             for (int z = y0; z < mc; ++z) {
-              const S* trow = Tn + (long long)C_[z] * dB + c0;
+              const S* trow = Tn + (long long)C_[z] * dB;
               S tv[4];
 #pragma unroll
-              for (int u = 0; u < 4; ++u) tv[u] = (c0 + u < dB) ? trow[u] : (S)0;
+              for (int u = 0; u < 4; ++u) tv[u] = trow[col[u]];
 #pragma unroll
               for (int v = 0; v < 4; ++v) {
                 const S rv = (y0 + v < kr) ? cvt<S>(rb[(long long)(y0 + v) * mc + z]) : (S)0;
@@ -858,11 +880,13 @@ template <class T, class S> struct Engine : Chain<T, S> {
               if (y0 + v < kr)
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
-                  if (c0 + u < dB) G[(long long)(kof + y0 + v) * dB + c0 + u] = acc[v][u];
+                  if (c0 + u < nc) G[(long long)(kof + y0 + v) * dB + col[u]] = acc[v][u];
           }
           kof += kr;
+          fl += 2.0 * nc * kr * mc;
+          __syncthreads();  // rl is rewritten by the next sector's list
         }
-        this->count(0, 2.0 * dB * rsz);
+        this->count(0, fl);
       }
       __syncthreads();
       // charges and flux of the new bond: Q side -r, R side +r
@@ -932,6 +956,7 @@ template <class T, class S> struct Engine : Chain<T, S> {
       __shared__ T* s_xp[kMaxSec];  // A, then Q (len x nv, column-major)
       __shared__ T* s_bp[kMaxSec];  // B = R^T vectors, rotated into W (nv x nv)
       __shared__ T* s_jp[kMaxSec];  // J (nv x nv)
+      __shared__ long long s_smused;  // shared memory taken by the sectors staged there
       T* Wl = at<T>(sl.o_W);                         // lenvec, packed at s_xo
       T* Wn = at<T>(sl.o_W) + (long long)chi() * chi();  // nvvec, packed at s_vo
       int* perm = order + md.cut;                    // pivots of the current sector (<= chi entries)
@@ -953,6 +978,7 @@ template <class T, class S> struct Engine : Chain<T, S> {
             s_jp[t] = Rb + s_vo[t];
           }
         }
+        s_smused = used;
       }
       __syncthreads();
       for (int t = 0; t < ns; ++t) {
@@ -1028,7 +1054,10 @@ template <class T, class S> struct Engine : Chain<T, S> {
           tau[k] = tk[k];
         }
         __syncthreads();
-        block_orgqr_cm(len, nv, x, tau);
+        if (x >= sm && x < sm + smcap)
+          block_orgqr_cm(len, nv, x, tau);
+        else  // staged in the slot: panels through the shared memory the staged sectors leave free
+          block_orgqr_panel(len, nv, x, tau, red, sm + s_smused, smcap - s_smused);
         const T* J = s_jp[t];
         const T* b = s_bp[t];
         T* lv = Wl + s_xo[t];
@@ -1103,37 +1132,55 @@ template <class T, class S> struct Engine : Chain<T, S> {
       t0 = tic();
       // U*S normalised before the absorption (exact; the product needs no second pass)
       expo += block_normalize(Rb, (long long)rows * c, red);
-      // new T[i-1] (A d x c) = T[i-1] * US, summing only over the rows of each kept vector's sector
+      // new T[i-1] (A d x c) = T[i-1] * US, summing only over the rows of each kept vector's sector.
+      // Per sector, the rows (a, d) of T[i-1] that can be nonzero in its columns R_ carry one charge:
+      // they are listed (in the X area, free after the output stage) with the sector's kept columns (in
+      // `order`, free after the selection), and only those outputs are computed; the rest stay zero.
       {
-        const int Ad = s_dA[i - 1] * s_dd[i - 1];
+        const int dP = s_dd[i - 1], Ad = s_dA[i - 1] * dP;
         const S* Tp = Tbuf(s_buf[i - 1]);
         S* out = Tbuf(spare2);
-        // a thread computes kCB consecutive rows xr of one column k (one load of U*S per kCB products)
-        const int xb = (Ad + kCB - 1) / kCB;
-        for (long long e = threadIdx.x; e < (long long)xb * c; e += blockDim.x) {
-          const int x0 = (int)(e / c) * kCB, k = (int)(e % c);
-          const int t = s_kmap[k];
+        const int* qLp = tqL(i - 1);
+        const int* qDp = tqD(i - 1);
+        const int* qRp = tqR(i - 1);
+        const int Fp = s_fl[i - 1];
+        int* xl = at<int>(sl.o_X);
+        int* kl = order;
+        for (long long e = threadIdx.x; e < (long long)Ad * c; e += blockDim.x) out[e] = (S)0;
+        __syncthreads();
+        double fl = 0;
+        for (int t = 0; t < ns; ++t) {
           const int* R_ = rl + s_sec.ro[t];
           const int mr = s_sec.m[t];
-          S acc[kCB];
-          const S* tp[kCB];
+          const int nk = block_compact(c, [&](int k) { return s_kmap[k] == t; }, kl, s_sh);
+          if (nk == 0) continue;
+          const int want = Fp - qRp[R_[0]];
+          const int nx = block_compact(
+              Ad, [&](int x) { return qLp[x / dP] + qDp[x % dP] == want; }, xl, s_sh);
+          // a thread computes kCB listed rows of one kept column (one load of U*S per kCB products)
+          const int xb = (nx + kCB - 1) / kCB;
+          for (long long e = threadIdx.x; e < (long long)xb * nk; e += blockDim.x) {
+            const int j0 = (int)(e / nk) * kCB, k = kl[e % nk];
+            S acc[kCB];
+            const S* tp[kCB];
 #pragma unroll
-          for (int v = 0; v < kCB; ++v) {
-            acc[v] = 0;
-            tp[v] = Tp + (long long)(x0 + v < Ad ? x0 + v : Ad - 1) * rows;
+            for (int v = 0; v < kCB; ++v) {
+              acc[v] = 0;
+              tp[v] = Tp + (long long)xl[j0 + v < nx ? j0 + v : nx - 1] * rows;
+            }
+            for (int q = 0; q < mr; ++q) {
+              const int rq = R_[q];
+              const S us = cvt<S>(Rb[(long long)rq * c + k]);
+#pragma unroll
+              for (int v = 0; v < kCB; ++v) acc[v] = fma(tp[v][rq], us, acc[v]);
+            }
+#pragma unroll
+            for (int v = 0; v < kCB; ++v)
+              if (j0 + v < nx) out[(long long)xl[j0 + v] * c + k] = acc[v];
           }
-          for (int q = 0; q < mr; ++q) {
-            const int rq = R_[q];
-            const S us = cvt<S>(Rb[(long long)rq * c + k]);
-#pragma unroll
-            for (int v = 0; v < kCB; ++v) acc[v] = fma(tp[v][rq], us, acc[v]);
-          }
-#pragma unroll
-          for (int v = 0; v < kCB; ++v)
-            if (x0 + v < Ad) out[(long long)(x0 + v) * c + k] = acc[v];
+          fl += 2.0 * nx * nk * mr;
+          __syncthreads();  // the lists are rewritten for the next sector
         }
-        double fl = 0;
-        for (int k = 0; k < c; ++k) fl += 2.0 * Ad * s_sec.m[s_kmap[k]];
         this->count(0, fl);
       }
       {

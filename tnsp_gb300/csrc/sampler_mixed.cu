@@ -1,5 +1,7 @@
 // mixed instantiation of the sampler kernels (double-float factorisations; float32 storage and
 // contractions) and its host launch wrappers.
+#include <mutex>
+
 #include "launch.h"
 
 namespace tnsp {
@@ -17,7 +19,14 @@ void launch_amplitude_mx(int grid, size_t smem, cudaStream_t st, const Model& md
                                                             confs, out_m, out_e, status);
 }
 
+// The limit is a property of the kernel function, shared by every context of the process: it is only
+// ever raised, so a context planned with less dynamic shared memory never lowers it under another
+// context that launches with more.
 cudaError_t set_smem_limit_mx(int bytes) {
+  static std::mutex mu;
+  static int current = -1;
+  std::lock_guard<std::mutex> lock(mu);
+  if (bytes <= current) return cudaSuccess;
   cudaError_t e = cudaFuncSetAttribute(sweep_kernel<dd, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(sweep_kernel<dd, float>, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -27,6 +36,7 @@ cudaError_t set_smem_limit_mx(int bytes) {
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(amplitude_kernel<dd, float>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              cudaSharedmemCarveoutMaxShared);
+  if (e == cudaSuccess) current = bytes;
   return e;
 }
 
