@@ -189,7 +189,7 @@ template <class T> __device__ int block_normalize(T* x, long n, T* red) {
 // round-robin (circle) order, one kJG-lane group per pair.  Returns the number of sweeps, or -1 if
 // the sweep limit was reached without convergence.
 template <class T>
-__device__ int block_jacobi(int nv, int len, T* X, T* Vr, int max_sweeps) {
+__device__ __noinline__ int block_jacobi(int nv, int len, T* X, T* Vr, int max_sweeps) {
   __shared__ int s_rot;
   for (long t = threadIdx.x; t < (long)nv * nv; t += blockDim.x) Vr[t] = (t / nv == t % nv) ? (T)1 : (T)0;
   __syncthreads();
@@ -316,7 +316,7 @@ __device__ __forceinline__ void apply_reflector_cm(int m, int r0, const T* v, bo
 }
 
 // G: m x n column-major (ld = m), overwritten by R (upper triangle) and the reflectors below it.
-template <class T> __device__ void block_geqrf_cm(int m, int n, T* G, T* tau, T* red) {
+template <class T> __device__ __noinline__ void block_geqrf_cm(int m, int n, T* G, T* tau, T* red) {
   const int kk = m < n ? m : n;
   __shared__ T s_beta, s_tau, s_scale;
   for (int j = 0; j < kk; ++j) {
@@ -351,7 +351,7 @@ template <class T> __device__ void block_geqrf_cm(int m, int n, T* G, T* tau, T*
 }
 
 // Forms Q (m x k, first k columns of G, column-major) in place from block_geqrf_cm's reflectors.
-template <class T> __device__ void block_orgqr_cm(int m, int k, T* G, const T* tau) {
+template <class T> __device__ __noinline__ void block_orgqr_cm(int m, int k, T* G, const T* tau) {
   for (int i = k - 1; i >= 0; --i) {
     T* gi = G + (long)i * m;
     const T ti = tau[i];
@@ -501,7 +501,7 @@ template <class T> __device__ void panel_explicit(int pm, int jb, T* P) {
 }
 
 // block_geqrf_cm for G in global memory, blocked through the shared staging P (pcap elements).
-template <class T> __device__ void block_geqrf_panel(int m, int n, T* G, T* tau, T* red, T* P, long pcap) {
+template <class T> __device__ __noinline__ void block_geqrf_panel(int m, int n, T* G, T* tau, T* red, T* P, long pcap) {
   const int nb = panel_width(m, pcap);
   if (nb < 2) {
     block_geqrf_cm(m, n, G, tau, red);
@@ -531,7 +531,7 @@ template <class T> __device__ void block_geqrf_panel(int m, int n, T* G, T* tau,
 // block_orgqr_cm for G in global memory, blocked through the shared staging P (pcap elements):
 // panels from the last one back, each applied to the columns already formed to its right and then
 // formed itself in shared memory.
-template <class T> __device__ void block_orgqr_panel(int m, int k, T* G, const T* tau, T* red, T* P, long pcap) {
+template <class T> __device__ __noinline__ void block_orgqr_panel(int m, int k, T* G, const T* tau, T* red, T* P, long pcap) {
   const int nb = panel_width(m, pcap);
   if (nb < 2) {
     block_orgqr_cm(m, k, G, tau);
@@ -573,7 +573,7 @@ template <class T> __device__ void block_orgqr_panel(int m, int k, T* G, const T
 // the number of barriers is set by the largest set instead of the sum over sets.  Pairs of a round
 // are spread over kJG-lane groups of all warps.  Returns the largest sweep count, or -1 if a set hit max_sweeps.
 template <class T, int MAXS>
-__device__ int block_jacobi_multi(int ns, const int* nv, const int* len, T* const* Xs, T* const* Vs, int max_sweeps) {
+__device__ __noinline__ int block_jacobi_multi(int ns, const int* nv, const int* len, T* const* Xs, T* const* Vs, int max_sweeps) {
   __shared__ int s_np[MAXS], s_pp[MAXS + 1], s_rot[MAXS], s_done[MAXS], s_sweeps[MAXS];
   __shared__ T s_noise[MAXS];
   __shared__ int s_active, s_fail;
@@ -674,7 +674,7 @@ __device__ int block_jacobi_multi(int ns, const int* nv, const int* len, T* cons
 // G: m x n column-major (m >= n).  At step j the remaining column of largest norm (rows j..m) is
 // swapped into position j (ties to the lower index); perm[j] records the original column.  On exit
 // R is in the upper triangle and the reflectors below it, as in block_geqrf_cm.
-template <class T> __device__ void block_geqp3_cm(int m, int n, T* G, T* tau, int* perm, T* red) {
+template <class T> __device__ __noinline__ void block_geqp3_cm(int m, int n, T* G, T* tau, int* perm, T* red) {
   __shared__ T s_beta, s_tau, s_scale;
   __shared__ int s_piv;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;

@@ -294,7 +294,7 @@ constexpr int kCB = 4;
 
 // out[(x*l + y), dd, (z*r + w)] = sum_p line[x, p, z] * W(p, dd, y, w); a thread computes kCB values of dd
 template <class T>
-__device__ void two_line(const T* __restrict__ line, Dims3 ld, const T* __restrict__ A, SiteView w, T* __restrict__ out) {
+__device__ __noinline__ void two_line(const T* __restrict__ line, Dims3 ld, const T* __restrict__ A, SiteView w, T* __restrict__ out) {
   const int Am = ld.a * w.dl, Bm = ld.b * w.dr;
   const int ddb = (w.dd + kCB - 1) / kCB;
   const long long n = (long long)Am * ddb * Bm;
@@ -327,7 +327,7 @@ __device__ void two_line(const T* __restrict__ line, Dims3 ld, const T* __restri
 
 // E'[a, r, b] = sum E[x, y, z] up[x, u, a] W(u, d, y, r) dn[z, d, b]
 template <class T>
-__device__ void strip_left(const T* E, int X, int Y, int Z, const T* up, Dims3 ud, const T* A, SiteView w,
+__device__ __noinline__ void strip_left(const T* E, int X, int Y, int Z, const T* up, Dims3 ud, const T* A, SiteView w,
                            const T* dn, Dims3 dd, T* t1, T* t2, T* out) {
   const int U = ud.p, Aa = ud.b, D = dd.p, Bb = dd.b, R = w.dr;
   const int ab = (Aa + kCB - 1) / kCB, bb = (Bb + kCB - 1) / kCB;
@@ -406,7 +406,7 @@ __device__ void strip_left(const T* E, int X, int Y, int Z, const T* up, Dims3 u
 
 // F'[x, l, z] = sum F[a, r, b] up[x, u, a] W(u, d, l, r) dn[z, d, b]
 template <class T>
-__device__ void strip_right(const T* F, int Aa, int R, int Bb, const T* up, Dims3 ud, const T* A, SiteView w,
+__device__ __noinline__ void strip_right(const T* F, int Aa, int R, int Bb, const T* up, Dims3 ud, const T* A, SiteView w,
                             const T* dn, Dims3 dd, T* s1, T* s2, T* out) {
   const int X = ud.a, U = ud.p, Z = dd.a, D = dd.p, L = w.dl;
   const int bb = (Bb + kCB - 1) / kCB, zb = (Z + kCB - 1) / kCB;
@@ -489,7 +489,7 @@ __device__ void strip_right(const T* F, int Aa, int R, int Bb, const T* up, Dims
 
 // h[u, d, l, r] = sum E[x, l, z] up[x, u, a] dn[z, d, b] F[a, r, b]
 template <class T>
-__device__ void strip_hole(const T* E, int X, int L, int Z, const T* up, Dims3 ud, const T* dn, Dims3 dd, const T* F,
+__device__ __noinline__ void strip_hole(const T* E, int X, int L, int Z, const T* up, Dims3 ud, const T* dn, Dims3 dd, const T* F,
                            int R, T* h1, T* h2, T* out) {
   const int U = ud.p, Aa = ud.b, D = dd.p, Bb = dd.b;
   const int ab = (Aa + kCB - 1) / kCB, bb = (Bb + kCB - 1) / kCB, rb = (R + kCB - 1) / kCB;
@@ -699,7 +699,7 @@ template <class T, class S> struct Engine : Chain<T, S> {
   // Every QR and SVD is done per charge sector (TAT/include/TAT/implement/qr.hpp:310-510,
   // svd.hpp:259-532); the SVD truncation keeps the `cut` largest singular values over all
   // sectors (svd.hpp:429-470).  Without symmetry every charge is zero: one sector.
-  __device__ void compress(int f, int idx) {
+  __device__ __noinline__ void compress(int f, int idx) {
     this->count(CT_COMPRESS, 1.0);
     const int n = nsites_along(f);
     const int prev = (f == F_UP || f == F_LEFT) ? idx - 1 : idx + 1;
@@ -1231,7 +1231,7 @@ template <class T, class S> struct Engine : Chain<T, S> {
   }
 
   // make line (f, idx) valid for the current configuration (recomputing its invalid upstreams)
-  __device__ void ensure(int f, int idx) {
+  __device__ __noinline__ void ensure(int f, int idx) {
     if (is_ones(f, idx)) return;
     const bool forward = (f == F_UP || f == F_LEFT);
     if (valid[f * kMaxL + idx]) return;
@@ -1333,7 +1333,7 @@ template <class T, class S> struct Engine : Chain<T, S> {
   }
 
   // build the strip (kind, idx) for the current configuration: all F, E[0]
-  __device__ void strip_begin(int kind, int idx) {
+  __device__ __noinline__ void strip_begin(int kind, int idx) {
     ensure(fup(kind), idx - 1);
     ensure(fdn(kind), idx + 1);
     const int n = strip_len(kind);
@@ -1361,7 +1361,7 @@ template <class T, class S> struct Engine : Chain<T, S> {
     __syncthreads();
   }
 
-  __device__ void strip_advance(int kind, int idx, int c) {
+  __device__ __noinline__ void strip_advance(int kind, int idx, int c) {
     // make E[c] valid
     while (*strip_eupto < c) {
       const int k = *strip_eupto;
@@ -1376,7 +1376,7 @@ template <class T, class S> struct Engine : Chain<T, S> {
   }
 
   // amplitude with columns c, c+1 of the strip set to s0, s1 (E[c] and F[c+2] valid)
-  __device__ void strip_replace2(int kind, int idx, int c, int s0, int s1, double& m, int& ex) {
+  __device__ __noinline__ void strip_replace2(int kind, int idx, int c, int s0, int s1, double& m, int& ex) {
     S* w0 = at<S>(sl.o_w0);
     S* w1 = at<S>(sl.o_w1);
     const int mp0 = strip_prefix(kind, idx, c);  // the pair's second site counts the first one's new value
@@ -1389,7 +1389,7 @@ template <class T, class S> struct Engine : Chain<T, S> {
   }
 
   // hole(()) = _inline_right_to_left[0, 0]: the row-0 strip (single_layer_auxiliaries.py:710-720)
-  __device__ void hole0(double& m, int& ex) {
+  __device__ __noinline__ void hole0(double& m, int& ex) {
     ensure(F_DOWN, 1);
     const int n = md.L2;
     S* f0 = at<S>(sl.o_w0);
@@ -1476,7 +1476,7 @@ __host__ __device__ inline double fermion_term_sign(const short* conf, int L1, i
 
 // one Metropolis proposal on the term at (kind, idx, c)-(kind, idx, c+1)
 template <class T, class S>
-__device__ void single_term(Engine<T, S>& eng, const Model& md, int kind, int idx, int c, int t, uint64_t* mt, int* s_mti,
+__device__ __noinline__ void single_term(Engine<T, S>& eng, const Model& md, int kind, int idx, int c, int t, uint64_t* mt, int* s_mti,
                             double* s_ws_m, int* s_ws_e, int* s_h0_valid, double* s_h0_m, int* s_h0_e, int64_t* accepted) {
   __shared__ int s_sel, s_nn, s_acc, s_skip;
   __shared__ double s_m;
