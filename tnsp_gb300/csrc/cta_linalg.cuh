@@ -171,7 +171,7 @@ template <class T> __device__ T block_max(T v, T* red) {
 
 // Rescales x[0..n) by a power of two so that max|x| lies in [0.5, 1); returns the exponent e with
 // x_old = x_new * 2^e (exact: a power-of-two scaling never rounds).  All-zero input: e = 0.
-template <class T> __device__ int block_normalize(T* x, long n, T* red) {
+template <class T> __device__ __noinline__ int block_normalize(T* x, long n, T* red) {
   T m = 0;
   for (long i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, fabs(x[i]));
   m = block_max(m, red);
@@ -290,7 +290,8 @@ template <class Pred> __device__ int block_compact(int n, Pred pred, int* out, i
 }
 
 // ---------------------------------------------------------------------------------------------
-// column-major Householder QR (LAPACK geqr2 / org2r conventions, any orthogonal gauge is fine)
+// column-major Householder QR (LAPACK geqr2 conventions, any orthogonal gauge is fine); Q is never
+// formed: its reflectors are applied where it is used (block_ormqr_panel in sampler_kernels.cuh)
 // ---------------------------------------------------------------------------------------------
 // Applies the reflector H = I - tau v v^T to columns c0..n-1 of the column-major m-row matrix G, one
 // kJG-lane group per column.  v occupies rows r0..m-1 of column-major storage `v`; with unit_head
@@ -350,30 +351,12 @@ template <class T> __device__ __noinline__ void block_geqrf_cm(int m, int n, T* 
   }
 }
 
-// Forms Q (m x k, first k columns of G, column-major) in place from block_geqrf_cm's reflectors.
-template <class T> __device__ __noinline__ void block_orgqr_cm(int m, int k, T* G, const T* tau) {
-  for (int i = k - 1; i >= 0; --i) {
-    T* gi = G + (long)i * m;
-    const T ti = tau[i];
-    if (i < k - 1) {
-      if (threadIdx.x == 0) gi[i] = (T)1;
-      __syncthreads();
-      if (ti != (T)0) apply_reflector_cm(m, i, gi, false, ti, G, i + 1, k);
-      __syncthreads();
-    }
-    for (int r = i + 1 + threadIdx.x; r < m; r += blockDim.x) gi[r] *= -ti;
-    for (int r = threadIdx.x; r < i; r += blockDim.x) gi[r] = (T)0;
-    if (threadIdx.x == 0) gi[i] = (T)1 - ti;
-    __syncthreads();
-  }
-}
-
 // ---------------------------------------------------------------------------------------------
 // blocked Householder QR for matrices staged in global memory (compact WY form of a panel:
 // H_0 H_1 ... H_{b-1} = I - V Tw V^T, LAPACK larft / larfb)
 // ---------------------------------------------------------------------------------------------
 // The unblocked routines above read and write the whole trailing matrix once per reflector; from
-// global memory that is one latency-bound pass per column.  The panel routines factorise (or form)
+// global memory that is one latency-bound pass per column.  The panel routines factorise (or apply)
 // up to kNB columns at a time in shared memory and apply them to the rest of the matrix as one block
 // reflector: two reads and one write of each trailing column per panel, with kNB independent dot
 // products per lane in flight.  Results equal the unblocked ones up to rounding (same reflectors).
@@ -527,41 +510,6 @@ template <class T> __device__ __noinline__ void block_geqrf_panel(int m, int n, 
     }
   }
 }
-
-// block_orgqr_cm for G in global memory, blocked through the shared staging P (pcap elements):
-// panels from the last one back, each applied to the columns already formed to its right and then
-// formed itself in shared memory.
-template <class T> __device__ __noinline__ void block_orgqr_panel(int m, int k, T* G, const T* tau, T* red, T* P, long pcap) {
-  const int nb = panel_width(m, pcap);
-  if (nb < 2) {
-    block_orgqr_cm(m, k, G, tau);
-    return;
-  }
-  for (int j0 = ((k - 1) / nb) * nb; j0 >= 0; j0 -= nb) {
-    const int jb = k - j0 < nb ? k - j0 : nb, pm = m - j0;
-    const long goff = (long)j0 * m + j0;
-    T* Y = P + (long)pm * jb;
-    T* Tw = Y + kNB * kNB;
-    panel_copy(m, pm, jb, G, goff, P, true);
-    __syncthreads();
-    panel_explicit(pm, jb, P);
-    __syncthreads();
-    if (j0 + jb < k) {
-      panel_tw(pm, jb, P, tau + j0, Y, Tw);
-      apply_panel<T, false>(pm, jb, P, Tw, G + j0, m, j0 + jb, k);
-      __syncthreads();
-    }
-    block_orgqr_cm(pm, jb, P, tau + j0);  // ends with a barrier
-    panel_copy(m, pm, jb, G, goff, P, false);
-    for (long e = threadIdx.x; e < (long)jb * j0; e += blockDim.x) {  // rows above the panel
-      const int c = (int)(e / j0), r = (int)(e % j0);
-      G[(long)(j0 + c) * m + r] = (T)0;
-    }
-    __syncthreads();
-  }
-}
-
-
 
 // ---------------------------------------------------------------------------------------------
 // one-sided Jacobi on several independent vector sets at once

@@ -112,6 +112,10 @@ struct Slots {
   long long capB, capT, capR, capE, capS, capH;  // capacities in elements
   // S-typed: o_lines, o_T, o_E, o_F, o_t1, o_t2, o_w0, o_w1, o_h; T-typed: o_G, o_R, o_tau, o_X, o_V, o_W, o_sig
   long long o_T, o_G, o_R, o_tau, o_X, o_V, o_W, o_sig, o_E, o_F, o_t1, o_t2, o_w0, o_w1, o_h;
+  // implicit Q of the QR sweep per site: o_qsec (int) [site][1 + 5 kMaxSec]: sector count, then per
+  // sector rows, reflectors, bond offset, row-list offset, reflector offset; o_qrow (int)
+  // [site][chi*Dmax]: row lists; o_qtau (T) [site][chi]: reflector scalars
+  long long o_qsec, o_qrow, o_qtau;
   int* ldims;               // [slot][4][kMaxL][kMaxL][3]
   int* lexp;                // [slot][4][kMaxL]
   int* order;               // [slot][cut*(Dmax+1)]: kept singular values, then pivots
@@ -142,6 +146,53 @@ template <> struct Cvt<dd> {
   static __device__ __forceinline__ dd from(double x) { return dd(x); }
 };
 template <class To, class From> __device__ __forceinline__ To cvt(From x) { return Cvt<To>::from(x); }
+
+// B <- Q B for the m x nc column-major matrix B (ld m), Q = H_0 H_1 ... H_{k-1} from block_geqrf_cm's
+// reflectors V (m x k column-major, stored as S; the unit diagonal is implicit and the entries above it
+// are not read) and their scalars tau (LAPACK ormqr, side L, no transpose).  Panels of up to kNB
+// reflectors, the last panel first, are staged in shared memory P (pcap elements) and applied as one
+// block reflector each; without room for a panel, one reflector at a time.  Ends with a barrier.
+template <class T, class S>
+__device__ __noinline__ void block_ormqr_panel(int m, int k, const S* V, const T* tau, T* B, int nc, T* P, long pcap) {
+  const int nb = panel_width(m, pcap);
+  if (nb < 2) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, grp = lane / kJG, sl = lane % kJG;
+    for (int y = k - 1; y >= 0; --y) {
+      const T ty = tau[y];
+      if (ty != (T)0) {
+        const S* v = V + (long)y * m;
+        for (int base = w * (32 / kJG); base < nc; base += kWarps * (32 / kJG)) {  // warp-uniform
+          const int c = base + grp;
+          const bool act = c < nc;
+          T* bc = B + (long)(act ? c : base) * m;
+          T d = (act && sl == 0) ? bc[y] : (T)0;
+          if (act)
+            for (int r = y + 1 + sl; r < m; r += kJG) d = fma(cvt<T>(v[r]), bc[r], d);
+          d = group_sum<kJG>(d) * ty;
+          if (act) {
+            if (sl == 0) bc[y] -= d;
+            for (int r = y + 1 + sl; r < m; r += kJG) bc[r] -= d * cvt<T>(v[r]);
+          }
+        }
+      }
+      __syncthreads();
+    }
+    return;
+  }
+  for (int j0 = ((k - 1) / nb) * nb; j0 >= 0; j0 -= nb) {
+    const int jb = k - j0 < nb ? k - j0 : nb, pm = m - j0;
+    T* Y = P + (long)pm * jb;
+    T* Tw = Y + kNB * kNB;
+    for (long e = threadIdx.x; e < (long)pm * jb; e += blockDim.x) {  // explicit unit-lower panel
+      const int c = (int)(e / pm), r = (int)(e % pm);
+      P[e] = r < c ? (T)0 : (r == c ? (T)1 : cvt<T>(V[(long)(j0 + c) * m + j0 + r]));
+    }
+    __syncthreads();
+    panel_tw(pm, jb, P, tau + j0, Y, Tw);
+    apply_panel<T, false>(pm, jb, P, Tw, B + j0, m, 0, nc);
+    __syncthreads();
+  }
+}
 
 // ------------------------------------------------------------------------------------------
 // random numbers: std::mt19937_64 + libstdc++ 13 distributions (thread 0 only)
@@ -762,15 +813,30 @@ template <class T, class S> struct Engine : Chain<T, S> {
       int ktot = 0;
       for (int t = 0; t < ns; ++t) ktot += min(s_sec.m[t], s_sec.c[t]);
       const int spare = s_buf[n], spare2 = s_buf[n + 1];
-      S* Tq = Tbuf(spare);   // new T[i] = Q (rows x ktot)
+      // new T[i] = Q is kept implicit: the buffer holds the sectors' reflectors, packed, and Q is applied
+      // to U*S in the SVD sweep (the only use of T[i] before it is replaced), so it is never formed
+      S* Tq = Tbuf(spare);
       S* G = Tbuf(spare2);   // new T[i+1] = R T[i+1]
       T* Gs = at<T>(sl.o_G);  // sector staging when shared memory is too small
-      for (long long t = threadIdx.x; t < (long long)rows * ktot; t += blockDim.x) Tq[t] = (S)0;
+      int* qsec = at<int>(sl.o_qsec) + (long long)i * (1 + 5 * kMaxSec);
+      int* qrow = at<int>(sl.o_qrow) + (long long)i * chi() * md.Dmax;
+      T* qtau = at<T>(sl.o_qtau) + (long long)i * chi();
       if (threadIdx.x == 0) {
-        int o = 0;
+        int o = 0, ko = 0, ro = 0, vo = 0;
+        qsec[0] = ns;
         for (int t = 0; t < ns; ++t) {
+          const int kr = min(s_sec.m[t], s_sec.c[t]);
           s_roffs[t] = o;
-          o += min(s_sec.m[t], s_sec.c[t]) * s_sec.c[t];
+          o += kr * s_sec.c[t];
+          int* q = qsec + 1 + 5 * t;
+          q[0] = s_sec.m[t];
+          q[1] = kr;
+          q[2] = ko;
+          q[3] = ro;
+          q[4] = vo;
+          ko += kr;
+          ro += s_sec.m[t];
+          vo += s_sec.m[t] * kr;
         }
       }
       __syncthreads();
@@ -799,7 +865,7 @@ template <class T, class S> struct Engine : Chain<T, S> {
           block_geqrf_panel(mr, mc, g, tau, red, sm, smcap);
         {
           const double mm = mr > mc ? mr : mc, nn = kr;
-          this->count(1, 2.0 * (2.0 * mm * nn * nn - 2.0 * nn * nn * nn / 3.0));
+          this->count(1, 2.0 * mm * nn * nn - 2.0 * nn * nn * nn / 3.0);
         }
         // R (kr x mc, row-major) into Rb
         T* rb = Rb + s_roffs[t];
@@ -807,14 +873,14 @@ template <class T, class S> struct Engine : Chain<T, S> {
           const int y = (int)(e / mc), z = (int)(e % mc);
           rb[e] = z >= y ? g[(long long)z * mr + y] * rsc : (T)0;
         }
-        __syncthreads();
-        if (g == sm)
-          block_orgqr_cm(mr, kr, g, tau);
-        else
-          block_orgqr_panel(mr, kr, g, tau, red, sm, smcap);
-        for (long long e = threadIdx.x; e < (long long)mr * kr; e += blockDim.x) {
-          const int y = (int)(e / mr), x = (int)(e % mr);
-          Tq[(long long)R_[x] * ktot + koff + y] = cvt<S>(g[e]);
+        // the reflectors (the first kr columns of g; R above their diagonal is not read again), their
+        // scalars and the sector's rows are kept for the application of Q in the SVD sweep
+        {
+          const int* q = qsec + 1 + 5 * t;
+          S* vq = Tq + q[4];
+          for (long long e = threadIdx.x; e < (long long)mr * kr; e += blockDim.x) vq[e] = cvt<S>(g[e]);
+          for (int x = threadIdx.x; x < mr; x += blockDim.x) qrow[q[3] + x] = R_[x];
+          for (int y = threadIdx.x; y < kr; y += blockDim.x) qtau[koff + y] = tau[y];
         }
         for (int y = threadIdx.x; y < kr; y += blockDim.x) {
           s_kmap[koff + y] = (short)t;
@@ -1043,39 +1109,6 @@ template <class T, class S> struct Engine : Chain<T, S> {
         }
       }
       __syncthreads();
-      // per sector: Q from the reflectors, lenvec = Q J, nvvec = P W
-      for (int t = 0; t < ns; ++t) {
-        const int nv = s_nvv[t], len = s_lenv[t];
-        T* x = s_xp[t];
-        int* pk = reinterpret_cast<int*>(Wn + s_vo[t]);
-        T* tk = Wl + s_xo[t];
-        for (int k = threadIdx.x; k < nv; k += blockDim.x) {
-          perm[k] = pk[k];
-          tau[k] = tk[k];
-        }
-        __syncthreads();
-        if (x >= sm && x < sm + smcap)
-          block_orgqr_cm(len, nv, x, tau);
-        else  // staged in the slot: panels through the shared memory the staged sectors leave free
-          block_orgqr_panel(len, nv, x, tau, red, sm + s_smused, smcap - s_smused);
-        const T* J = s_jp[t];
-        const T* b = s_bp[t];
-        T* lv = Wl + s_xo[t];
-        T* nvv = Wn + s_vo[t];
-        for (long long e = threadIdx.x; e < (long long)nv * len; e += blockDim.x) {
-          const int j = (int)(e / len), q = (int)(e % len);
-          const T* Jj = J + (long long)j * nv;
-          T acc = 0;
-          for (int k = 0; k < nv; ++k) acc = fma(x[(long long)k * len + q], Jj[k], acc);
-          lv[e] = acc;
-        }
-        const T ssc = (T)ldexp(1.0, s_esec[t]);
-        for (long long e = threadIdx.x; e < (long long)nv * nv; e += blockDim.x) {
-          const int j = (int)(e / nv), k = (int)(e % nv);
-          nvv[(long long)j * nv + perm[k]] = b[e] * ssc;
-        }
-        __syncthreads();
-      }
       const int c = md.cut < nsv ? md.cut : nsv;
       // global selection: descending value, ties to the earlier sector / lower index
       for (int j = threadIdx.x; j < nsv; j += blockDim.x) {
@@ -1095,6 +1128,46 @@ template <class T, class S> struct Engine : Chain<T, S> {
         while (t + 1 < ns && s_so[t + 1] <= j) ++t;
         s_kmap[k] = (short)t;
         s_kloc[k] = (short)(j - s_so[t]);
+      }
+      __syncthreads();
+      // per sector: nvvec = P W for every value, lenvec = Q J only for the kept ones: Q is applied by its
+      // reflectors (ormqr) to those rows of J, staged in the G area, never formed
+      for (int t = 0; t < ns; ++t) {
+        const int nv = s_nvv[t], len = s_lenv[t];
+        const T* x = s_xp[t];
+        int* pk = reinterpret_cast<int*>(Wn + s_vo[t]);
+        T* tk = Wl + s_xo[t];
+        for (int k = threadIdx.x; k < nv; k += blockDim.x) {
+          perm[k] = pk[k];
+          tau[k] = tk[k];
+        }
+        __syncthreads();
+        const T* J = s_jp[t];
+        const T* b = s_bp[t];
+        T* lv = Wl + s_xo[t];
+        T* nvv = Wn + s_vo[t];
+        const T ssc = (T)ldexp(1.0, s_esec[t]);
+        for (long long e = threadIdx.x; e < (long long)nv * nv; e += blockDim.x) {
+          const int j = (int)(e / nv), k = (int)(e % nv);
+          nvv[(long long)j * nv + perm[k]] = b[e] * ssc;
+        }
+        int* kl = order;  // kept vectors of this sector (order is free after the selection)
+        const int nk = block_compact(c, [&](int k) { return s_kmap[k] == t; }, kl, s_sh);
+        if (nk > 0) {
+          T* Bs = at<T>(sl.o_G);
+          for (long long e = threadIdx.x; e < (long long)nk * len; e += blockDim.x) {
+            const int p = (int)(e / len), q = (int)(e % len);
+            Bs[e] = q < nv ? J[(long long)s_kloc[kl[p]] * nv + q] : (T)0;
+          }
+          __syncthreads();
+          // panels in the shared memory the staged sectors leave free
+          block_ormqr_panel(len, nv, x, tau, Bs, nk, sm + s_smused, smcap - s_smused);
+          for (long long e = threadIdx.x; e < (long long)nk * len; e += blockDim.x) {
+            const int p = (int)(e / len), q = (int)(e % len);
+            lv[(long long)s_kloc[kl[p]] * len + q] = Bs[e];
+          }
+        }
+        __syncthreads();
       }
       T smax = 0;
       for (int j = threadIdx.x; j < nsv; j += blockDim.x) smax = fmax(smax, sig[j]);
@@ -1132,56 +1205,45 @@ template <class T, class S> struct Engine : Chain<T, S> {
       t0 = tic();
       // U*S normalised before the absorption (exact; the product needs no second pass)
       expo += block_normalize(Rb, (long long)rows * c, red);
-      // new T[i-1] (A d x c) = T[i-1] * US, summing only over the rows of each kept vector's sector.
-      // Per sector, the rows (a, d) of T[i-1] that can be nonzero in its columns R_ carry one charge:
-      // they are listed (in the X area, free after the output stage) with the sector's kept columns (in
-      // `order`, free after the selection), and only those outputs are computed; the rest stay zero.
+      // new T[i-1] (A d x c) = Q_{i-1} US with Q_{i-1} from its reflectors (LAPACK ormqr): per QR sector
+      // of step i-1, the rows of US on its bonds are nonzero only in the kept columns of the bonds'
+      // charge; that block is staged (in the G area), padded to the sector's rows, Q_t is applied to it
+      // and the result goes to the sector's rows of T[i-1].  Rows in no sector stay zero.
       {
-        const int dP = s_dd[i - 1], Ad = s_dA[i - 1] * dP;
-        const S* Tp = Tbuf(s_buf[i - 1]);
+        const int Ad = s_dA[i - 1] * s_dd[i - 1];
+        const S* Vq = Tbuf(s_buf[i - 1]);
         S* out = Tbuf(spare2);
-        const int* qLp = tqL(i - 1);
-        const int* qDp = tqD(i - 1);
-        const int* qRp = tqR(i - 1);
-        const int Fp = s_fl[i - 1];
-        int* xl = at<int>(sl.o_X);
-        int* kl = order;
+        const int* qsec = at<int>(sl.o_qsec) + (long long)(i - 1) * (1 + 5 * kMaxSec);
+        const int* qrow = at<int>(sl.o_qrow) + (long long)(i - 1) * chi() * md.Dmax;
+        const T* qtau = at<T>(sl.o_qtau) + (long long)(i - 1) * chi();
+        const int* qbond = tqL(i);  // charges of the bonds (the rows of T[i] and of US)
+        T* Bs = at<T>(sl.o_G);
+        int* kl = order;  // free after the selection above
         for (long long e = threadIdx.x; e < (long long)Ad * c; e += blockDim.x) out[e] = (S)0;
         __syncthreads();
+        const int nq = qsec[0];
         double fl = 0;
-        for (int t = 0; t < ns; ++t) {
-          const int* R_ = rl + s_sec.ro[t];
-          const int mr = s_sec.m[t];
-          const int nk = block_compact(c, [&](int k) { return s_kmap[k] == t; }, kl, s_sh);
+        for (int t = 0; t < nq; ++t) {
+          const int* q = qsec + 1 + 5 * t;
+          const int mr = q[0], kr = q[1], ko = q[2];
+          const int* Rq = qrow + q[3];
+          const int rq = qbond[ko];
+          const int nk = block_compact(c, [&](int k) { return s_sec.r[s_kmap[k]] == rq; }, kl, s_sh);
           if (nk == 0) continue;
-          const int want = Fp - qRp[R_[0]];
-          const int nx = block_compact(
-              Ad, [&](int x) { return qLp[x / dP] + qDp[x % dP] == want; }, xl, s_sh);
-          // a thread computes kCB listed rows of one kept column (one load of U*S per kCB products)
-          const int xb = (nx + kCB - 1) / kCB;
-          for (long long e = threadIdx.x; e < (long long)xb * nk; e += blockDim.x) {
-            const int j0 = (int)(e / nk) * kCB, k = kl[e % nk];
-            S acc[kCB];
-            const S* tp[kCB];
-#pragma unroll
-            for (int v = 0; v < kCB; ++v) {
-              acc[v] = 0;
-              tp[v] = Tp + (long long)xl[j0 + v < nx ? j0 + v : nx - 1] * rows;
-            }
-            for (int q = 0; q < mr; ++q) {
-              const int rq = R_[q];
-              const S us = cvt<S>(Rb[(long long)rq * c + k]);
-#pragma unroll
-              for (int v = 0; v < kCB; ++v) acc[v] = fma(tp[v][rq], us, acc[v]);
-            }
-#pragma unroll
-            for (int v = 0; v < kCB; ++v)
-              if (j0 + v < nx) out[(long long)xl[j0 + v] * c + k] = acc[v];
+          for (long long e = threadIdx.x; e < (long long)mr * nk; e += blockDim.x) {
+            const int j = (int)(e / mr), x = (int)(e % mr);
+            Bs[e] = x < kr ? Rb[(long long)(ko + x) * c + kl[j]] : (T)0;
           }
-          fl += 2.0 * nx * nk * mr;
-          __syncthreads();  // the lists are rewritten for the next sector
+          __syncthreads();
+          block_ormqr_panel(mr, kr, Vq + q[4], qtau + ko, Bs, nk, sm, smcap);
+          for (long long e = threadIdx.x; e < (long long)mr * nk; e += blockDim.x) {
+            const int j = (int)(e / mr), x = (int)(e % mr);
+            out[(long long)Rq[x] * c + kl[j]] = cvt<S>(Bs[e]);
+          }
+          fl += 4.0 * mr * kr * nk;
+          __syncthreads();  // Bs and the column list are reused by the next sector
         }
-        this->count(0, fl);
+        this->count(1, fl);
       }
       {
         int* qLi = tqL(i);
@@ -1292,7 +1354,7 @@ template <class T, class S> struct Engine : Chain<T, S> {
   }
 
   // E[c+1] = E[c] x column c (physical index s); writes into dst with exponent returned
-  __device__ int step_left(int kind, int idx, int c, const S* Ein, Dims3 e, int s, S* dst, int mp = 0) {
+  __device__ __noinline__ int step_left(int kind, int idx, int c, const S* Ein, Dims3 e, int s, S* dst, int mp = 0) {
     const long long t0 = tic();
     int l1, l2;
     strip_site_rc(kind, idx, c, l1, l2);
@@ -1306,7 +1368,7 @@ template <class T, class S> struct Engine : Chain<T, S> {
     toc(PH_STRIP, t0);
     return ex;
   }
-  __device__ int step_right(int kind, int idx, int c, const S* Fin, Dims3 f, int s, S* dst, int mp = 0) {
+  __device__ __noinline__ int step_right(int kind, int idx, int c, const S* Fin, Dims3 f, int s, S* dst, int mp = 0) {
     const long long t0 = tic();
     int l1, l2;
     strip_site_rc(kind, idx, c, l1, l2);
