@@ -133,7 +133,7 @@ __device__ __forceinline__ bool jacobi_pair(bool act, T* xi, T* xj, int len, T* 
   const T c = (T)1 / sqrt((T)1 + t * t);
   const T s = c * t;
   rotate_group<G>(c, s, xi, xj, len, sl);
-  rotate_group<G>(c, s, vi, vj, n, sl);
+  if (vi) rotate_group<G>(c, s, vi, vj, n, sl);  // no accumulation when the caller passes none
   return true;
 }
 
@@ -185,13 +185,14 @@ template <class T> __device__ __noinline__ int block_normalize(T* x, long n, T* 
 }
 
 // One-sided (Hestenes) Jacobi on nv vectors X[j][0..len) (vector-major), accumulating the same
-// rotations into Vr[j][0..nv) (initialised to the identity here).  Pairs are visited in the
+// rotations into Vr[j][0..nv) (initialised to the identity here; Vr = nullptr: not accumulated).  Pairs are visited in the
 // round-robin (circle) order, one kJG-lane group per pair.  Returns the number of sweeps, or -1 if
 // the sweep limit was reached without convergence.
 template <class T>
 __device__ __noinline__ int block_jacobi(int nv, int len, T* X, T* Vr, int max_sweeps) {
   __shared__ int s_rot;
-  for (long t = threadIdx.x; t < (long)nv * nv; t += blockDim.x) Vr[t] = (t / nv == t % nv) ? (T)1 : (T)0;
+  if (Vr)
+    for (long t = threadIdx.x; t < (long)nv * nv; t += blockDim.x) Vr[t] = (t / nv == t % nv) ? (T)1 : (T)0;
   __syncthreads();
   if (nv < 2) return 0;
   const int np = nv + (nv & 1);  // padded to even; index nv is a dummy
@@ -227,8 +228,8 @@ __device__ __noinline__ int block_jacobi(int nv, int len, T* X, T* Vr, int max_s
           act = i < nv && j < nv;
         }
         if (!act) i = j = 0;
-        if (jacobi_pair<kJG>(act, X + (long)i * len, X + (long)j * len, len, Vr + (long)i * nv, Vr + (long)j * nv, nv,
-                             noise2, tol, sl))
+        if (jacobi_pair<kJG>(act, X + (long)i * len, X + (long)j * len, len, Vr ? Vr + (long)i * nv : nullptr,
+                             Vr ? Vr + (long)j * nv : nullptr, nv, noise2, tol, sl))
           rot = 1;
       }
       __syncthreads();
@@ -515,7 +516,8 @@ template <class T> __device__ __noinline__ void block_geqrf_panel(int m, int n, 
 // one-sided Jacobi on several independent vector sets at once
 // ---------------------------------------------------------------------------------------------
 // Set t has nv[t] vectors of length len[t] at Xs[t] (vector-major) and accumulates its rotations
-// into Vs[t] (nv[t] x nv[t], set to the identity here); each set may live in shared or global memory.  Every set follows its own
+// into Vs[t] (nv[t] x nv[t], set to the identity here; Vs = nullptr: not accumulated); each set may
+// live in shared or global memory.  Every set follows its own
 // circle ordering and convergence test (rotation rule and tolerance of block_jacobi, noise floor
 // tol^2 * |A|_F^2), but all sets advance together: a block barrier ends one round of every set, so
 // the number of barriers is set by the largest set instead of the sum over sets.  Pairs of a round
@@ -526,9 +528,10 @@ __device__ __noinline__ int block_jacobi_multi(int ns, const int* nv, const int*
   __shared__ T s_noise[MAXS];
   __shared__ int s_active, s_fail;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int t = 0; t < ns; ++t)
-    for (long e = threadIdx.x; e < (long)nv[t] * nv[t]; e += blockDim.x)
-      Vs[t][e] = (e / nv[t] == e % nv[t]) ? (T)1 : (T)0;
+  if (Vs)
+    for (int t = 0; t < ns; ++t)
+      for (long e = threadIdx.x; e < (long)nv[t] * nv[t]; e += blockDim.x)
+        Vs[t][e] = (e / nv[t] == e % nv[t]) ? (T)1 : (T)0;
   // squared Frobenius norm of each set (invariant under the rotations, >= sigma_max^2): the noise
   // floor below which a vector is left alone is tol^2 * |A|_F^2
   if (threadIdx.x < MAXS) s_noise[threadIdx.x] = 0;
@@ -578,8 +581,8 @@ __device__ __noinline__ int block_jacobi_multi(int ns, const int* nv, const int*
       const int L = act ? len[t] : 0, n = act ? nv[t] : 0;
       T* xi = act ? Xs[t] + (long)i * L : nullptr;
       T* xj = act ? Xs[t] + (long)j * L : nullptr;
-      T* vi = act ? Vs[t] + (long)i * n : nullptr;
-      T* vj = act ? Vs[t] + (long)j * n : nullptr;
+      T* vi = (act && Vs) ? Vs[t] + (long)i * n : nullptr;
+      T* vj = (act && Vs) ? Vs[t] + (long)j * n : nullptr;
       const T tol = Eps<T>::value() * (T)(L > 32 ? L : 32);
       const T noise = act ? s_noise[t] : (T)0;
       if (jacobi_pair<kJG>(act, xi, xj, L, vi, vj, n, noise, tol, sl) && sl == 0) s_rot[t] = 1;

@@ -1013,38 +1013,41 @@ template <class T, class S> struct Engine : Chain<T, S> {
       const S* M = Tbuf(s_buf[i]);
       // QR-preconditioned one-sided Jacobi (Drmac-Veselic): per sector, A (len x nv, its columns are
       // the block's columns when it is tall, its rows when wide) = Q R P^T by Householder QR with
-      // column pivoting, then one-sided Jacobi on the nv columns of R^T (accumulating J), which
-      // converges in fewer sweeps and on vectors of length nv.  With B = R^T, B J = W:
+      // column pivoting, then one-sided Jacobi on the nv columns of R^T, which converges in fewer
+      // sweeps and on vectors of length nv.  With B = R^T and B J = W (J the product of the rotations):
       //   A = (Q J) Sigma (P W Sigma^-1)^T,  sigma_j = |W_j|.
-      // Outputs per kept value j: lenvec_j = (Q J)_j (len-dim, unit) and nvvec_j = P W_j (nv-dim,
-      // sigma_j times unit).  Sector data sit in shared memory while it has room, else in the slot.
+      // Outputs per value j: nvvec_j = P W_j (nv-dim, sigma_j times unit) and, for the kept values only,
+      // lenvec_j = (Q J)_j = A nvvec_j / sigma_j^2 (len-dim, unit), so neither J nor Q is formed.
+      // Sector data sit in shared memory while it has room (the Jacobi vectors first), else in the slot.
       __shared__ int s_nvv[kMaxSec], s_lenv[kMaxSec], s_esec[kMaxSec];
-      __shared__ T* s_xp[kMaxSec];  // A, then Q (len x nv, column-major)
+      __shared__ T* s_xp[kMaxSec];  // A, then R and the reflectors (len x nv, column-major)
       __shared__ T* s_bp[kMaxSec];  // B = R^T vectors, rotated into W (nv x nv)
-      __shared__ T* s_jp[kMaxSec];  // J (nv x nv)
-      __shared__ long long s_smused;  // shared memory taken by the sectors staged there
       T* Wl = at<T>(sl.o_W);                         // lenvec, packed at s_xo
       T* Wn = at<T>(sl.o_W) + (long long)chi() * chi();  // nvvec, packed at s_vo
       int* perm = order + md.cut;                    // pivots of the current sector (<= chi entries)
       if (threadIdx.x == 0) {
         long long used = 0;
-        for (int t = 0; t < ns; ++t) {
+        for (int t = 0; t < ns; ++t) {  // the Jacobi vectors first: every sweep reads and rotates them
           const int nv = min(s_sec.m[t], s_sec.c[t]), len = max(s_sec.m[t], s_sec.c[t]);
           s_nvv[t] = nv;
           s_lenv[t] = len;
-          const long long need = (long long)nv * len + 2LL * nv * nv;
-          if (used + need <= smcap) {
-            s_xp[t] = sm + used;
-            s_bp[t] = sm + used + (long long)nv * len;
-            s_jp[t] = sm + used + (long long)nv * len + (long long)nv * nv;
-            used += need;
+          const long long nb = (long long)nv * nv;
+          if (used + nb <= smcap) {
+            s_bp[t] = sm + used;
+            used += nb;
           } else {
-            s_xp[t] = X + s_xo[t];
             s_bp[t] = V + s_vo[t];
-            s_jp[t] = Rb + s_vo[t];
           }
         }
-        s_smused = used;
+        for (int t = 0; t < ns; ++t) {  // then the blocks of the pivoted QR
+          const long long nx = (long long)s_nvv[t] * s_lenv[t];
+          if (used + nx <= smcap) {
+            s_xp[t] = sm + used;
+            used += nx;
+          } else {
+            s_xp[t] = X + s_xo[t];
+          }
+        }
       }
       __syncthreads();
       for (int t = 0; t < ns; ++t) {
@@ -1075,20 +1078,15 @@ template <class T, class S> struct Engine : Chain<T, S> {
           const int i = (int)(e / nv), k = (int)(e % nv);
           b[e] = k >= i ? x[(long long)k * len + i] : (T)0;
         }
-        // keep the pivots and reflector scalars of this sector next to its J block (J is set up by
-        // the Jacobi routine later): store them in the packed nvvec area, which is written last
+        // keep the pivots of this sector in its packed nvvec area, which is written last
         int* pk = reinterpret_cast<int*>(Wn + s_vo[t]);
-        T* tk = Wl + s_xo[t];
-        for (int k = threadIdx.x; k < nv; k += blockDim.x) {
-          pk[k] = perm[k];
-          tk[k] = tau[k];
-        }
+        for (int k = threadIdx.x; k < nv; k += blockDim.x) pk[k] = perm[k];
         __syncthreads();
       }
       toc(PH_SVDOUT, t0);  // gather + pivoted QR
       t0 = tic();
-      const int sweeps = ns == 1 ? block_jacobi(s_nvv[0], s_nvv[0], s_bp[0], s_jp[0], md.jacobi_max)
-                                 : block_jacobi_multi<T, kMaxSec>(ns, s_nvv, s_nvv, s_bp, s_jp, md.jacobi_max);
+      const int sweeps = ns == 1 ? block_jacobi(s_nvv[0], s_nvv[0], s_bp[0], (T*)nullptr, md.jacobi_max)
+                                 : block_jacobi_multi<T, kMaxSec>(ns, s_nvv, s_nvv, s_bp, nullptr, md.jacobi_max);
       toc(PH_JACOBI, t0);
       t0 = tic();
       if (sweeps < 0 && threadIdx.x == 0) atomicOr(status, ST_SVD_NOCONV);
@@ -1130,19 +1128,23 @@ template <class T, class S> struct Engine : Chain<T, S> {
         s_kloc[k] = (short)(j - s_so[t]);
       }
       __syncthreads();
-      // per sector: nvvec = P W for every value, lenvec = Q J only for the kept ones: Q is applied by its
-      // reflectors (ormqr) to those rows of J, staged in the G area, never formed
+      T smax = 0;
+      for (int j = threadIdx.x; j < nsv; j += blockDim.x) smax = fmax(smax, sig[j]);
+      smax = block_max(smax, red);
+      int lmaxi = 1;
+      for (int t = 0; t < ns; ++t) lmaxi = max(lmaxi, max(s_sec.m[t], s_sec.c[t]));
+      const T thr = smax * Eps<T>::value() * (T)lmaxi;
+      // per sector: nvvec = P W for every value; lenvec_j = A nvvec_j / sigma_j^2 for the kept ones
+      // (zero below the noise floor thr, where the value carries no direction), A read back from the
+      // compression tensor; each thread computes kCB kept vectors at one position (one load of A each)
       for (int t = 0; t < ns; ++t) {
         const int nv = s_nvv[t], len = s_lenv[t];
-        const T* x = s_xp[t];
-        int* pk = reinterpret_cast<int*>(Wn + s_vo[t]);
-        T* tk = Wl + s_xo[t];
-        for (int k = threadIdx.x; k < nv; k += blockDim.x) {
-          perm[k] = pk[k];
-          tau[k] = tk[k];
-        }
+        const bool caseA = s_sec.c[t] <= s_sec.m[t];
+        const int* R_ = rl + s_sec.ro[t];
+        const int* C_ = cl + s_sec.co[t];
+        const int* pk = reinterpret_cast<const int*>(Wn + s_vo[t]);
+        for (int k = threadIdx.x; k < nv; k += blockDim.x) perm[k] = pk[k];
         __syncthreads();
-        const T* J = s_jp[t];
         const T* b = s_bp[t];
         T* lv = Wl + s_xo[t];
         T* nvv = Wn + s_vo[t];
@@ -1152,29 +1154,33 @@ template <class T, class S> struct Engine : Chain<T, S> {
           nvv[(long long)j * nv + perm[k]] = b[e] * ssc;
         }
         int* kl = order;  // kept vectors of this sector (order is free after the selection)
-        const int nk = block_compact(c, [&](int k) { return s_kmap[k] == t; }, kl, s_sh);
-        if (nk > 0) {
-          T* Bs = at<T>(sl.o_G);
-          for (long long e = threadIdx.x; e < (long long)nk * len; e += blockDim.x) {
-            const int p = (int)(e / len), q = (int)(e % len);
-            Bs[e] = q < nv ? J[(long long)s_kloc[kl[p]] * nv + q] : (T)0;
+        const int nk = block_compact(c, [&](int k) { return s_kmap[k] == t; }, kl, s_sh);  // ends with a barrier
+        const int kb = (nk + kCB - 1) / kCB;
+        for (long long e = threadIdx.x; e < (long long)kb * len; e += blockDim.x) {
+          const int p0 = (int)(e / len) * kCB, q = (int)(e % len);
+          int jv[kCB];
+          T acc[kCB];
+          const T* nj[kCB];
+#pragma unroll
+          for (int v = 0; v < kCB; ++v) {
+            jv[v] = s_kloc[kl[p0 + v < nk ? p0 + v : nk - 1]];
+            nj[v] = nvv + (long long)jv[v] * nv;
+            acc[v] = 0;
           }
-          __syncthreads();
-          // panels in the shared memory the staged sectors leave free
-          block_ormqr_panel(len, nv, x, tau, Bs, nk, sm + s_smused, smcap - s_smused);
-          for (long long e = threadIdx.x; e < (long long)nk * len; e += blockDim.x) {
-            const int p = (int)(e / len), q = (int)(e % len);
-            lv[(long long)s_kloc[kl[p]] * len + q] = Bs[e];
+          for (int r = 0; r < nv; ++r) {
+            const T a = cvt<T>(caseA ? M[(long long)R_[q] * cols + C_[r]] : M[(long long)R_[r] * cols + C_[q]]);
+#pragma unroll
+            for (int v = 0; v < kCB; ++v) acc[v] = fma(a, nj[v][r], acc[v]);
           }
+#pragma unroll
+          for (int v = 0; v < kCB; ++v)
+            if (p0 + v < nk) {
+              const T sv = sig[s_so[t] + jv[v]];
+              lv[(long long)jv[v] * len + q] = sv > thr ? acc[v] / (sv * sv) : (T)0;
+            }
         }
         __syncthreads();
       }
-      T smax = 0;
-      for (int j = threadIdx.x; j < nsv; j += blockDim.x) smax = fmax(smax, sig[j]);
-      smax = block_max(smax, red);
-      int lmaxi = 1;
-      for (int t = 0; t < ns; ++t) lmaxi = max(lmaxi, max(s_sec.m[t], s_sec.c[t]));
-      const T thr = smax * Eps<T>::value() * (T)lmaxi;
       const int spare = s_buf[n], spare2 = s_buf[n + 1];
       S* Tn = Tbuf(spare);  // new T[i] (c x cols)
       for (long long e = threadIdx.x; e < (long long)c * cols; e += blockDim.x) Tn[e] = (S)0;
