@@ -343,10 +343,56 @@ template <class T, class S> struct Chain {
 // and guarded writes; each output's sum runs over its terms in the same order as a one-output loop.
 constexpr int kCB = 4;
 
-// out[(x*l + y), dd, (z*r + w)] = sum_p line[x, p, z] * W(p, dd, y, w); a thread computes kCB values of dd
+// out[(x*l + y), dd, (z*r + w)] = sum_p line[x, p, z] * W(p, dd, y, w).
+// With `dense`, every output (a thread computes kCB values of dd).  Otherwise only the charge-allowed
+// outputs, qa[x] + ql[y] + qd[dd] + qb[z] + qr[w] == F (qa, qb null: zero), are computed and written,
+// and the other entries of `out` are left as they are: the compression reads this tensor only at
+// allowed entries (its sector gathers and the R absorption's column lists), and a block tensor has
+// most of its entries outside them.  A thread takes one (row, column) pair and its allowed dd, kTL at
+// a time.
+constexpr int kTL = 2;
 template <class T>
-__device__ __noinline__ void two_line(const T* __restrict__ line, Dims3 ld, const T* __restrict__ A, SiteView w, T* __restrict__ out) {
+__device__ __noinline__ void two_line(const T* __restrict__ line, Dims3 ld, const T* __restrict__ A, SiteView w,
+                                      T* __restrict__ out, const int* qa, const int* qb, int F, bool dense) {
   const int Am = ld.a * w.dl, Bm = ld.b * w.dr;
+  if (!dense) {
+    const long long n = (long long)Am * Bm;
+    for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+      const int col = (int)(t % Bm), row = (int)(t / Bm);
+      const int x = row / w.dl, y = row % w.dl, z = col / w.dr, ww = col % w.dr;
+      const int want = F - (qa ? qa[x] : 0) - w.ql[y] - (qb ? qb[z] : 0) - w.qr[ww];
+      const T* lp = line + (long long)x * ld.p * ld.b + z;
+      const T* wb = A + w.base + (long long)y * w.sl + (long long)ww * w.sr;
+      int d0 = 0;
+      while (true) {
+        int ds[kTL];
+#pragma unroll
+        for (int v = 0; v < kTL; ++v) {  // the next kTL allowed dd from d0 on (-1: none)
+          while (d0 < w.dd && w.qd[d0] != want) ++d0;
+          ds[v] = d0 < w.dd ? d0++ : -1;
+        }
+        if (ds[0] < 0) break;
+        T acc[kTL];
+        const T* wp[kTL];
+#pragma unroll
+        for (int v = 0; v < kTL; ++v) {
+          acc[v] = 0;
+          wp[v] = wb + (long long)(ds[v] >= 0 ? ds[v] : ds[0]) * w.sd;
+        }
+        for (int p = 0; p < ld.p; ++p) {
+          const T lv = lp[(long long)p * ld.b];
+#pragma unroll
+          for (int v = 0; v < kTL; ++v) acc[v] = fma(lv, wp[v][(long long)p * w.su], acc[v]);
+        }
+#pragma unroll
+        for (int v = 0; v < kTL; ++v)
+          if (ds[v] >= 0) out[((long long)row * w.dd + ds[v]) * Bm + col] = acc[v];
+        if (ds[kTL - 1] < 0) break;
+      }
+    }
+    __syncthreads();
+    return;
+  }
   const int ddb = (w.dd + kCB - 1) / kCB;
   const long long n = (long long)Am * ddb * Bm;
   for (long long t = threadIdx.x; t < n; t += blockDim.x) {
@@ -774,10 +820,12 @@ template <class T, class S> struct Engine : Chain<T, S> {
       const SiteView w = site(l1, l2, conf[l1 * md.L2 + l2], orient, prefix);
       prefix += conf[l1 * md.L2 + l2];
       const Dims3 ld = lsdim(f, prev, i);
-      two_line(lsite(f, prev, i), ld, A, w, Tbuf(s_buf[i]));
-      this->count(0, 2.0 * ld.a * w.dl * w.dd * ld.b * w.dr * ld.p);
       const int* qa = ones_prev ? nullptr : lqa(f, prev, i);
       const int* qb = ones_prev ? nullptr : lqb(f, prev, i);
+      // a one-site line is stored as is (its zeros included); longer ones only read allowed entries
+      two_line(lsite(f, prev, i), ld, A, w, Tbuf(s_buf[i]), qa, qb,
+               (ones_prev ? 0 : *lflux(f, prev, i)) + w.flux, n == 1);
+      this->count(0, 2.0 * ld.a * w.dl * w.dd * ld.b * w.dr * ld.p);
       int* L = tqL(i);
       int* Rr = tqR(i);
       int* Dd = tqD(i);
