@@ -386,6 +386,8 @@ def _roofline(workload, prec, counters, steps, launch_ms, samples_per_launch):
                                       "double-float multiply-add" if dd_like else
                                       "nominal FP64 1.25 TFLOP/s" if prec == TNSP_FP64 else "nominal FP32")},
         "phase_cycle_share": phase_share(cycles),
+        # counter slots 14 and 15: truncated SVDs and their Jacobi sweeps (max over a call's sectors)
+        "jacobi_sweeps_per_svd": float(counters[15] / counters[14]) if counters[14] > 0 else None,
     }
 
 
