@@ -90,7 +90,7 @@ DD_NOMINAL_GFLOPS = FP32_NOMINAL_GFLOPS / DD_FMA_INSTRUCTIONS
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per chain-sample of the sweep kernel, from
 # one ncu capture of a small launch of the same kernel and lattice (one sweep + observation of a few
 # dozen chains), divided by its chains: the traffic of a launch is the chains it processes times this
-MEASURED_DRAM_BYTES_PER_SAMPLE = {}
+MEASURED_DRAM_BYTES_PER_SAMPLE = {("heis8x8u1", "dd"): 1.187e9}  # 15.11 GB read + 22.88 GB written, 32 chains
 # seconds per sample of the oracle port over the reference's own compiled CPU path, one thread each, on
 # the 8x8 U(1) lattice (oracle/time_reference.py on an x86 core: reference 1.160 s, port 2.426 s)
 PORT_OVER_REFERENCE_TIME = 2.09
