@@ -280,8 +280,9 @@ int tnsp_counters_read(tnsp_ctx* ctx, double* flops, int reset);
  * Scratch comes from a 64 MiB array compiled into the library (held by every device that loads
  * it, until the process exits); cut * max bond extent above 1024, or a lattice/cut whose one-chain
  * scratch does not fit in it, returns TNSP_E_TOO_LARGE before any device work.  The first call on a
- * device resolves the array's device address (cudaGetSymbolAddress) with that device current: make
- * that first call before any stream capture begins.  All calls share the array, which keeps the last
+ * device resolves the array's device address (cudaGetSymbolAddress) with that device current.  No
+ * call can be captured into a CUDA graph: each copies host arrays to the device and waits for its
+ * stream.  All calls share the array, which keeps the last
  * call's contents (each call rewrites what must start at a known value): calls that overlap on the
  * GPU race and must be serialised.  On failure tnsp_last_error(NULL) gives the reason.
  */

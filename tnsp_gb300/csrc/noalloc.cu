@@ -20,9 +20,9 @@
 // streams, or different host threads) race on the arena and give undefined results: serialise them.
 //
 // Set-up: the first call on each device resolves the arena's device address with
-// cudaGetSymbolAddress (with that device current) and caches it; make that first call before any
-// stream capture begins.  The call itself copies small host arrays to the arena and waits for its
-// stream before it returns.
+// cudaGetSymbolAddress (with that device current) and caches it.  Every call copies small host
+// arrays to the arena and waits for its stream before it returns, so no call can be captured into a
+// CUDA graph.
 //
 // Errors: the reason of the calling thread's last failure is kept in a thread-local buffer and is
 // returned by tnsp_last_error(NULL).
