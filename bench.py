@@ -10,8 +10,8 @@ benchmark statement, C1..C5):
   heis4x4      C1: 4x4 Heisenberg (J=1), no symmetry, D=4, Dcut=16, tensors N(0,1)/sqrt(2 D^z),
                Neel start, 64 thermalisation sweeps, 1024 chains
   heis8x8u1    C2 (default): 8x8 Heisenberg, U(1) bonds {-1:2, 0:2, +1:2} (D=6), Dcut=36, blocks
-               N(0,1), Neel start (total Sz = 0), 456 chains = one resident wave of 3 blocks x 152 SMs
-               (a 4096-sample launch runs the same kernel for nine waves), 2 thermalisation sweeps
+               N(0,1), Neel start (total Sz = 0), 4096 chains = 4096 samples per step (the resident
+               blocks, 3 x 152 SMs, take the chains in nine waves), 2 thermalisation sweeps, 1 timed step
   tv8x8        C3: 8x8 spinless t-V (t = V = 1), Fermi U(1), 32 particles, bonds {Q-1:2, Q:4, Q+1:2}
                along the charge flow and {-1:2, 0:4, +1:2} on interior D bonds (D=8), Dcut=64; one
                resident wave of chains from random fillings with nonzero amplitude
@@ -57,8 +57,8 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     "heis4x4": dict(kind="heis", L1=4, L2=4, D=4, sectors=None, cut=16, scale=True, chains=1024, therm=64, steps=5,
                     precision="fp64", config="C1"),
-    "heis8x8u1": dict(kind="heis", L1=8, L2=8, D=6, sectors=(2, 2, 2), cut=36, scale=False, chains=456, therm=2,
-                      steps=2, precision="dd", config="C2"),
+    "heis8x8u1": dict(kind="heis", L1=8, L2=8, D=6, sectors=(2, 2, 2), cut=36, scale=False, chains=4096, therm=2,
+                      steps=1, precision="dd", config="C2"),
     "tv8x8": dict(kind="tv", L1=8, L2=8, D=(2, 4, 2), interior=((-1, 2), (0, 4), (1, 2)), particles=32, cut=64,
                   chains=0, therm=1, steps=1, precision="dd", config="C3"),
     "heis6x6u1d4": dict(kind="heis", L1=6, L2=6, D=4, sectors=(1, 2, 1), cut=16, scale=False, chains=2048, therm=2,
