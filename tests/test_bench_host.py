@@ -23,13 +23,12 @@ def test_tau_int_of_short_chains_with_different_means():
     assert tau < 0.7 and info["n_per_chain"] == 25 and info["chains"] == 456
 
 
-def test_tau_int_of_short_chains_with_different_means():
-    """Many short chains whose means differ (as chains still drifting after a short thermalisation):
-    subtracting each chain's own mean keeps the offsets out of the autocorrelation."""
-    rng = np.random.default_rng(2)
-    x = rng.normal(size=(25, 456)) + 3.0 * rng.normal(size=(1, 456))
-    tau, info = bench.tau_int(x)
-    assert tau < 0.7 and info["n_per_chain"] == 25 and info["chains"] == 456
+def test_default_workload_is_the_headline_configuration():
+    """The default step is config 2 as stated: 8x8 U(1) bonds {-1:2, 0:2, +1:2}, Dcut 36, 4096 samples,
+    at fixed error (double-float, checked against float64 in the line)."""
+    w = bench.WORKLOADS[bench.DEFAULT_WORKLOAD]
+    assert (w["L1"], w["L2"], w["D"], tuple(w["sectors"]), w["cut"]) == (8, 8, 6, (2, 2, 2), 36)
+    assert w["chains"] == 4096 and w["precision"] == "dd" and w["config"] == "C2"
 
 
 def test_tau_int_of_an_ar1_process():
