@@ -141,10 +141,11 @@ inline void plan_slots(const tnsp_ctx* c, Slots& s, long long tsize, long long s
   s.o_W = take(2 * chi * chi, tsize);
   s.o_sig = take(chi, tsize);
   // Q of each QR-sweep step, kept implicit (the reflectors stay in the site's compression buffer):
-  // per site its sector table, the sectors' row lists and the reflector scalars
-  s.o_qsec = take(Lmax * (1 + 5LL * kMaxSec), 4);
+  // per site its sector table, the sectors' row lists, the reflector scalars and the panels' Tw factors
+  s.o_qsec = take(Lmax * (1 + 6LL * kMaxSec), 4);
   s.o_qrow = take(Lmax * chi * D, 4);
   s.o_qtau = take(Lmax * chi, tsize);
+  s.o_qtw = take(Lmax * (chi + kMaxSec) * kNB * kNB, tsize);
   s.o_E = take((Lmax + 1) * s.capE, ssize);
   s.o_F = take((Lmax + 1) * s.capE, ssize);
   s.o_t1 = take(s.capS, ssize);

@@ -484,8 +484,10 @@ template <class T> __device__ void panel_explicit(int pm, int jb, T* P) {
   }
 }
 
-// block_geqrf_cm for G in global memory, blocked through the shared staging P (pcap elements).
-template <class T> __device__ __noinline__ void block_geqrf_panel(int m, int n, T* G, T* tau, T* red, T* P, long pcap) {
+// block_geqrf_cm for G in global memory, blocked through the shared staging P (pcap elements).  With
+// TwOut, the Tw factor of every panel (kNB x kNB, in panel order) is also written there.
+template <class T>
+__device__ __noinline__ void block_geqrf_panel(int m, int n, T* G, T* tau, T* red, T* P, long pcap, T* TwOut) {
   const int nb = panel_width(m, pcap);
   if (nb < 2) {
     block_geqrf_cm(m, n, G, tau, red);
@@ -502,11 +504,13 @@ template <class T> __device__ __noinline__ void block_geqrf_panel(int m, int n, 
     block_geqrf_cm(pm, jb, P, tau + j0, red);  // ends with a barrier
     panel_copy(m, pm, jb, G, goff, P, false);  // R's rows of the panel and its reflectors
     __syncthreads();
-    if (j0 + jb < n) {
+    if (j0 + jb < n || TwOut) {
       panel_explicit(pm, jb, P);
       __syncthreads();
-      panel_tw(pm, jb, P, tau + j0, Y, Tw);
-      apply_panel<T, true>(pm, jb, P, Tw, G + j0, m, j0 + jb, n);
+      panel_tw(pm, jb, P, tau + j0, Y, Tw);  // ends with a barrier
+      if (TwOut)
+        for (int e = threadIdx.x; e < kNB * kNB; e += blockDim.x) TwOut[(long)(j0 / nb) * kNB * kNB + e] = Tw[e];
+      if (j0 + jb < n) apply_panel<T, true>(pm, jb, P, Tw, G + j0, m, j0 + jb, n);
       __syncthreads();
     }
   }

@@ -112,10 +112,11 @@ struct Slots {
   long long capB, capT, capR, capE, capS, capH;  // capacities in elements
   // S-typed: o_lines, o_T, o_E, o_F, o_t1, o_t2, o_w0, o_w1, o_h; T-typed: o_G, o_R, o_tau, o_X, o_V, o_W, o_sig
   long long o_T, o_G, o_R, o_tau, o_X, o_V, o_W, o_sig, o_E, o_F, o_t1, o_t2, o_w0, o_w1, o_h;
-  // implicit Q of the QR sweep per site: o_qsec (int) [site][1 + 5 kMaxSec]: sector count, then per
-  // sector rows, reflectors, bond offset, row-list offset, reflector offset; o_qrow (int)
-  // [site][chi*Dmax]: row lists; o_qtau (T) [site][chi]: reflector scalars
-  long long o_qsec, o_qrow, o_qtau;
+  // implicit Q of the QR sweep per site: o_qsec (int) [site][1 + 6 kMaxSec]: sector count, then per
+  // sector rows, reflectors, bond offset, row-list offset, reflector offset, Tw offset (-1: none);
+  // o_qrow (int) [site][chi*Dmax]: row lists; o_qtau (T) [site][chi]: reflector scalars; o_qtw (T)
+  // [site][(chi + kMaxSec) kNB^2]: the Tw factor of every panel of the sectors factorised in panels
+  long long o_qsec, o_qrow, o_qtau, o_qtw;
   int* ldims;               // [slot][4][kMaxL][kMaxL][3]
   int* lexp;                // [slot][4][kMaxL]
   int* order;               // [slot][cut*(Dmax+1)]: kept singular values, then pivots
@@ -151,9 +152,12 @@ template <class To, class From> __device__ __forceinline__ To cvt(From x) { retu
 // reflectors V (m x k column-major, stored as S; the unit diagonal is implicit and the entries above it
 // are not read) and their scalars tau (LAPACK ormqr, side L, no transpose).  Panels of up to kNB
 // reflectors, the last panel first, are staged in shared memory P (pcap elements) and applied as one
-// block reflector each; without room for a panel, one reflector at a time.  Ends with a barrier.
+// block reflector each; without room for a panel, one reflector at a time.  TwIn, when given, holds
+// the panels' Tw factors (kNB x kNB each, in panel order) kept by the factorisation, which are then not
+// recomputed.  Ends with a barrier.
 template <class T, class S>
-__device__ __noinline__ void block_ormqr_panel(int m, int k, const S* V, const T* tau, T* B, int nc, T* P, long pcap) {
+__device__ __noinline__ void block_ormqr_panel(int m, int k, const S* V, const T* tau, T* B, int nc, T* P, long pcap,
+                                               const T* TwIn) {
   const int nb = panel_width(m, pcap);
   if (nb < 2) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, grp = lane / kJG, sl = lane % kJG;
@@ -188,8 +192,12 @@ __device__ __noinline__ void block_ormqr_panel(int m, int k, const S* V, const T
       P[e] = r < c ? (T)0 : (r == c ? (T)1 : cvt<T>(V[(long)(j0 + c) * m + j0 + r]));
     }
     __syncthreads();
-    panel_tw(pm, jb, P, tau + j0, Y, Tw);
-    apply_panel<T, false>(pm, jb, P, Tw, B + j0, m, 0, nc);
+    const T* tw = Tw;
+    if (TwIn)
+      tw = TwIn + (long)(j0 / nb) * kNB * kNB;
+    else
+      panel_tw(pm, jb, P, tau + j0, Y, Tw);
+    apply_panel<T, false>(pm, jb, P, tw, B + j0, m, 0, nc);
     __syncthreads();
   }
 }
@@ -866,22 +874,29 @@ template <class T, class S> struct Engine : Chain<T, S> {
       S* Tq = Tbuf(spare);
       S* G = Tbuf(spare2);   // new T[i+1] = R T[i+1]
       T* Gs = at<T>(sl.o_G);  // sector staging when shared memory is too small
-      int* qsec = at<int>(sl.o_qsec) + (long long)i * (1 + 5 * kMaxSec);
+      int* qsec = at<int>(sl.o_qsec) + (long long)i * (1 + 6 * kMaxSec);
       int* qrow = at<int>(sl.o_qrow) + (long long)i * chi() * md.Dmax;
       T* qtau = at<T>(sl.o_qtau) + (long long)i * chi();
+      T* qtw = at<T>(sl.o_qtw) + (long long)i * (chi() + kMaxSec) * kNB * kNB;
       if (threadIdx.x == 0) {
-        int o = 0, ko = 0, ro = 0, vo = 0;
+        int o = 0, ko = 0, ro = 0, vo = 0, wo = 0;
         qsec[0] = ns;
         for (int t = 0; t < ns; ++t) {
           const int kr = min(s_sec.m[t], s_sec.c[t]);
           s_roffs[t] = o;
           o += kr * s_sec.c[t];
-          int* q = qsec + 1 + 5 * t;
+          int* q = qsec + 1 + 6 * t;
           q[0] = s_sec.m[t];
           q[1] = kr;
           q[2] = ko;
           q[3] = ro;
           q[4] = vo;
+          // the panels' Tw factors are kept where the sector is factorised in panels and its reflectors
+          // are stored at the factorisation's precision (they must match the panels the factors belong to)
+          const int nb = panel_width(s_sec.m[t], smcap);
+          const bool panels = (long long)s_sec.m[t] * s_sec.c[t] > smcap && nb >= 2 && sizeof(S) == sizeof(T);
+          q[5] = panels ? wo : -1;
+          if (panels) wo += (kr + nb - 1) / nb * kNB * kNB;
           ko += kr;
           ro += s_sec.m[t];
           vo += s_sec.m[t] * kr;
@@ -910,7 +925,7 @@ template <class T, class S> struct Engine : Chain<T, S> {
         if (g == sm)
           block_geqrf_cm(mr, mc, g, tau, red);
         else
-          block_geqrf_panel(mr, mc, g, tau, red, sm, smcap);
+          block_geqrf_panel(mr, mc, g, tau, red, sm, smcap, qsec[1 + 6 * t + 5] >= 0 ? qtw + qsec[1 + 6 * t + 5] : nullptr);
         {
           const double mm = mr > mc ? mr : mc, nn = kr;
           this->count(1, 2.0 * mm * nn * nn - 2.0 * nn * nn * nn / 3.0);
@@ -924,7 +939,7 @@ template <class T, class S> struct Engine : Chain<T, S> {
         // the reflectors (the first kr columns of g; R above their diagonal is not read again), their
         // scalars and the sector's rows are kept for the application of Q in the SVD sweep
         {
-          const int* q = qsec + 1 + 5 * t;
+          const int* q = qsec + 1 + 6 * t;
           S* vq = Tq + q[4];
           for (long long e = threadIdx.x; e < (long long)mr * kr; e += blockDim.x) vq[e] = cvt<S>(g[e]);
           for (int x = threadIdx.x; x < mr; x += blockDim.x) qrow[q[3] + x] = R_[x];
@@ -1267,9 +1282,10 @@ template <class T, class S> struct Engine : Chain<T, S> {
         const int Ad = s_dA[i - 1] * s_dd[i - 1];
         const S* Vq = Tbuf(s_buf[i - 1]);
         S* out = Tbuf(spare2);
-        const int* qsec = at<int>(sl.o_qsec) + (long long)(i - 1) * (1 + 5 * kMaxSec);
+        const int* qsec = at<int>(sl.o_qsec) + (long long)(i - 1) * (1 + 6 * kMaxSec);
         const int* qrow = at<int>(sl.o_qrow) + (long long)(i - 1) * chi() * md.Dmax;
         const T* qtau = at<T>(sl.o_qtau) + (long long)(i - 1) * chi();
+        const T* qtw = at<T>(sl.o_qtw) + (long long)(i - 1) * (chi() + kMaxSec) * kNB * kNB;
         const int* qbond = tqL(i);  // charges of the bonds (the rows of T[i] and of US)
         T* Bs = at<T>(sl.o_G);
         int* kl = order;  // free after the selection above
@@ -1278,7 +1294,7 @@ template <class T, class S> struct Engine : Chain<T, S> {
         const int nq = qsec[0];
         double fl = 0;
         for (int t = 0; t < nq; ++t) {
-          const int* q = qsec + 1 + 5 * t;
+          const int* q = qsec + 1 + 6 * t;
           const int mr = q[0], kr = q[1], ko = q[2];
           const int* Rq = qrow + q[3];
           const int rq = qbond[ko];
@@ -1289,7 +1305,7 @@ template <class T, class S> struct Engine : Chain<T, S> {
             Bs[e] = x < kr ? Rb[(long long)(ko + x) * c + kl[j]] : (T)0;
           }
           __syncthreads();
-          block_ormqr_panel(mr, kr, Vq + q[4], qtau + ko, Bs, nk, sm, smcap);
+          block_ormqr_panel(mr, kr, Vq + q[4], qtau + ko, Bs, nk, sm, smcap, q[5] >= 0 ? qtw + q[5] : (const T*)nullptr);
           for (long long e = threadIdx.x; e < (long long)mr * nk; e += blockDim.x) {
             const int j = (int)(e / mr), x = (int)(e % mr);
             out[(long long)Rq[x] * c + kl[j]] = cvt<S>(Bs[e]);
